@@ -1,0 +1,151 @@
+/*
+ * pdos_gpu.h -- the C-ABI layer under pdos() and the GPU-only extensions.
+ *
+ * Everything here takes plain pointers and sizes.  The reference has no GPU
+ * layer; each entry point names the reference code whose work it carries.
+ * All functions return PDOSGPU_OK (0) or a negative status; the last error
+ * message of the calling thread is in pdos_gpu_last_error().
+ */
+#ifndef PDOS_GB300_PDOS_GPU_H
+#define PDOS_GB300_PDOS_GPU_H
+
+#include <stdint.h>
+
+#include "pdos.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PDOSGPU_OK = 0,
+  PDOSGPU_EINVAL = -1,   /* bad sizes, indices, cone table or parameters */
+  PDOSGPU_ENOMEM = -2,   /* host or device allocation failed */
+  PDOSGPU_ECUDA = -3,    /* a CUDA call failed */
+  PDOSGPU_ENOTSUP = -4   /* no usable GPU / unsupported request */
+};
+
+enum { PDOSGPU_FP64 = 0, PDOSGPU_FP32 = 1 };          /* storage/arithmetic */
+enum { PDOSGPU_SCALE_2NORM = 0, PDOSGPU_SCALE_RUIZ = 1 }; /* NORMALIZE=1 kind */
+
+typedef struct {
+  int precision;   /* PDOSGPU_FP64 (default): every operation in double, the
+                      reference's arithmetic.  PDOSGPU_FP32: A, vectors and
+                      SpMV in float; dot products, norms, CG scalars, the gap
+                      and the objective accumulated in double. */
+  int scaling;     /* equilibration used when NORMALIZE=1: PDOSGPU_SCALE_2NORM
+                      (common.h:69-162, the reference's default build) or
+                      PDOSGPU_SCALE_RUIZ (ruiz_equil_common.h:98-322) */
+  int device;      /* CUDA device ordinal (default 0) */
+  int reserved[5];
+} pdosgpu_options;
+
+typedef struct {
+  int64_t admm_iters;   /* ADMM iterations run (pdos.c:94 loop index at exit) */
+  int64_t cg_iters;     /* CG iterations summed over the solve */
+  int solved;           /* 1 = "Solved", 0 = "Indeterminate" */
+  int pad;
+  double p_res, d_res;  /* last DIMACS residuals (pdos.c:95-96), -1 if none */
+  double p_obj, d_obj, eta;
+  double lambda;        /* common.h:182 */
+  double setup_ms;      /* host wall time of pdosgpu_setup */
+  double solve_ms;      /* host wall time of the last pdosgpu_solve/iterate */
+  int64_t kernel_launches; /* kernels launched by this workspace so far
+                              (set-up excluded; graph nodes counted) */
+} pdosgpu_info;
+
+/* A problem with 64-bit indices in host memory: the fields of Data/Cone/
+ * Params flattened (pdos.h:15-35, cones.h:8-13). */
+typedef struct {
+  int64_t n, m;
+  const double *Ax;
+  const int64_t *Ai, *Ap;
+  const double *b, *c;
+  const double *x0, *y0, *s0;   /* warm start, each may be NULL */
+  int64_t f, l, qsize;
+  const int64_t *q;
+  int64_t max_iters, cg_max_its;
+  double eps_abs, alpha, cg_tol;
+  int64_t verbose, normalize;
+} pdosgpu_problem;
+
+typedef struct pdosgpu_work pdosgpu_work;
+
+const char *pdos_gpu_last_error(void);
+void pdosgpu_default_options(pdosgpu_options *opt);
+
+/* Workspace set-up: copies the problem to the GPU, builds the CSR of A on
+ * the device (cs_transpose, cs.c:146-168), equilibrates (common.h:35-218 /
+ * ruiz_equil_common.h:98-322), sets lambda and the x-space ratio and
+ * evaluates the residuals of the starting point.  Replaces initWork
+ * (indirect/private.c:3-14). */
+int pdosgpu_setup(const pdosgpu_problem *prob, const pdosgpu_options *opt,
+                  pdosgpu_work **out);
+
+/* Run ADMM iterations (pdos.c:94-120) until the DIMACS test passes or
+ * MAX_ITERS iterations have run in total. */
+int pdosgpu_solve(pdosgpu_work *w);
+
+/* Run at most `iters` more ADMM iterations (stops early when solved or at
+ * MAX_ITERS). */
+int pdosgpu_iterate(pdosgpu_work *w, int64_t iters);
+
+/* Restore the starting iterate (warm start or zeros); problem data and
+ * scaling stay resident. */
+int pdosgpu_reset(pdosgpu_work *w);
+
+/* Copy the unscaled solution (pdos.c:251-294) to host arrays of n, m, m
+ * doubles (any may be NULL) and fill *info (may be NULL). */
+int pdosgpu_fetch(pdosgpu_work *w, double *x, double *s, double *y,
+                  pdosgpu_info *info);
+
+void pdosgpu_free(pdosgpu_work *w);
+
+/* The CUDA stream (cudaStream_t) every kernel of this workspace runs on. */
+void *pdosgpu_stream(pdosgpu_work *w);
+
+/* Kernel timing for roofline reports: launch one of the iteration's SpMV
+ * kernels `reps` times back to back on the workspace stream between two
+ * CUDA events and return the mean duration in ms.  which: 0 = CG A pass
+ * (u = A p), 1 = CG A' pass (t = p + A'u), 2 = top A' pass on (y, u),
+ * 3 = post A pass.  Leaves the iterate undefined: call pdosgpu_reset()
+ * before solving again. */
+int pdosgpu_time_kernel(pdosgpu_work *w, int which, int reps, double *ms_per_launch);
+
+/* pdos() with explicit GPU options; info may be NULL. */
+Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt,
+             pdosgpu_info *info);
+
+/* ---- kernel-level entry points on device memory ------------------------
+ * Pointers are device pointers; `stream` is a cudaStream_t (NULL = legacy
+ * default stream).  They run asynchronously on `stream`. */
+
+/* CSC (m x n, int32 row indices) -> CSR of the same matrix, stable in column
+ * order: the index work of cs_transpose (cs.c:146-168) and cs_cumsum
+ * (cs.c:83-97), bit-exact.  Rp: m+1, Rj: nnz, Rx: nnz (Rx may be NULL when
+ * Ax is NULL).  Uses temporary device memory allocated internally. */
+int pdosgpu_csc_to_csr_f64(int32_t m, int32_t n, int32_t nnz, const int32_t *Ap,
+                           const int32_t *Ai, const double *Ax, int32_t *Rp,
+                           int32_t *Rj, double *Rx, void *stream);
+
+/* y = sc * M x (accum = 0) or y += sc * M x (accum != 0) for the row-wise
+ * matrix M (rows x cols, int32 rowptr/colidx).  The row gather of
+ * accumByScaledA / accumByScaledATrans (linAlg.h:70-115).  Allocates its
+ * tile table and long-row scratch internally. */
+int pdosgpu_spmv_f64(int32_t rows, int32_t cols, const int32_t *rowptr,
+                     const int32_t *colidx, const double *val, const double *x,
+                     double sc, double *y, int accum, void *stream);
+int pdosgpu_spmv_f32(int32_t rows, int32_t cols, const int32_t *rowptr,
+                     const int32_t *colidx, const float *val, const float *x,
+                     float sc, float *y, int accum, void *stream);
+
+/* In-place projection of v (m = f + l + sum q) onto {0}^f x R+^l x
+ * SOC(q[0]) x ... (projCone, cones.c:5-57).  q is a HOST array. */
+int pdosgpu_proj_cone_f64(double *v, int64_t f, int64_t l, int64_t qsize,
+                          const int64_t *q, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PDOS_GB300_PDOS_GPU_H */

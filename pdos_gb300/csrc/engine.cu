@@ -1,0 +1,904 @@
+// Grid engine: set-up on the device, one captured CUDA graph per ADMM
+// iteration, host loop that replays it until the device-side stop flag is
+// set.  Instantiated for double (the reference's arithmetic) and float
+// (float storage and SpMV, double reductions).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "engine.cuh"
+#include "setup_kernels.cuh"
+
+namespace pdosgpu {
+
+namespace {
+
+int g_num_sms = 0;
+
+int num_sms() {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+inline int grid1d(int64_t n, int block = 256) {
+  int64_t g = (n + block - 1) / block;
+  const int64_t cap = (int64_t)num_sms() * 16;
+  if (g > cap) g = cap;
+  return (int)(g < 1 ? 1 : g);
+}
+
+template <class K>
+int persistent_grid(K kernel, int block, size_t smem, int work) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (per_sm < 1) per_sm = 1;
+  int g = per_sm * num_sms();
+  if (work < g) g = work;
+  return g < 1 ? 1 : g;
+}
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- scan
+int device_excl_scan(const int *in, int n, int *out, bool with_total, DeviceArena &tmp,
+                     cudaStream_t st) {
+  using namespace setup;
+  if (n == 0) {
+    if (with_total) PDOS_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(int), st));
+    return PDOSGPU_OK;
+  }
+  const int nb = (n + kScanTile - 1) / kScanTile;
+  int *sums = nullptr;
+  PDOS_TRY(tmp.alloc(&sums, (size_t)nb + 1));
+  scan_tile_sums<<<nb, kScanBlock, 0, st>>>(in, n, sums);
+  scan_sums<<<1, kScanBlock, 0, st>>>(sums, nb);
+  scan_apply<<<nb, kScanBlock, 0, st>>>(in, n, sums, out, with_total ? 1 : 0);
+  PDOS_CUDA_TRY(cudaGetLastError());
+  return PDOSGPU_OK;
+}
+
+// Stable CSC -> CSR: Rp (m+1) and the permutation perm[k] = CSC position of
+// the k-th CSR entry; col_of[p] = column of CSC position p.
+int device_transpose(int m, int n, int nnz, const int32_t *Ap, const int32_t *Ai, int32_t *Rp,
+                     int32_t *perm, int32_t *col_of, DeviceArena &tmp, cudaStream_t st) {
+  using namespace setup;
+  int *cnt = nullptr;
+  PDOS_TRY(tmp.alloc(&cnt, (size_t)m));
+  PDOS_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)m, st));
+  if (nnz > 0) count_rows_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai, nnz, cnt);
+  PDOS_TRY(device_excl_scan(cnt, m, Rp, true, tmp, st));
+  if (nnz == 0) return PDOSGPU_OK;
+  col_of_kernel<<<grid1d(nnz), 256, 0, st>>>(Ap, n, nnz, col_of);
+  int32_t *ka, *kb, *va, *vb;
+  PDOS_TRY(tmp.alloc(&ka, (size_t)nnz));
+  PDOS_TRY(tmp.alloc(&kb, (size_t)nnz));
+  PDOS_TRY(tmp.alloc(&va, (size_t)nnz));
+  vb = perm;
+  PDOS_CUDA_TRY(cudaMemcpyAsync(ka, Ai, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToDevice, st));
+  iota_kernel<<<grid1d(nnz), 256, 0, st>>>(va, nnz);
+  int bits = 1;
+  while (bits < 31 && (1 << bits) < m) ++bits;
+  const int passes = (bits + 7) / 8;
+  const int nblocks = (nnz + kRadixTile - 1) / kRadixTile;
+  int *counts = nullptr;
+  PDOS_TRY(tmp.alloc(&counts, (size_t)kRadixBins * nblocks));
+  // ping-pong so that the last pass lands in `perm`
+  int32_t *bufs_k[2] = {ka, kb};
+  int32_t *bufs_v[2] = {va, vb};
+  if (passes % 2 == 0) {
+    bufs_v[0] = vb;
+    bufs_v[1] = va;
+    iota_kernel<<<grid1d(nnz), 256, 0, st>>>(vb, nnz);
+  }
+  for (int pass = 0; pass < passes; ++pass) {
+    const int src = pass & 1, dst = src ^ 1;
+    radix_hist<<<nblocks, kRadixBlock, 0, st>>>(bufs_k[src], nnz, pass * 8, counts, nblocks);
+    PDOS_TRY(device_excl_scan(counts, kRadixBins * nblocks, counts, false, tmp, st));
+    radix_scatter<<<nblocks, kRadixBlock, 0, st>>>(bufs_k[src], bufs_v[src], nnz, pass * 8, counts,
+                                                     nblocks, bufs_k[dst], bufs_v[dst]);
+  }
+  PDOS_CUDA_TRY(cudaGetLastError());
+  return PDOSGPU_OK;
+}
+
+// ============================================================== Engine<T>
+template <typename T>
+class Engine : public EngineBase {
+ public:
+  ~Engine() override {
+    if (exec_) cudaGraphExecDestroy(exec_);
+    for (auto e : extra_exec_)
+      if (e) cudaGraphExecDestroy(e);
+    if (stream_) {
+      cudaStreamSynchronize(stream_);
+      cudaStreamDestroy(stream_);
+    }
+    if (host_state_) cudaFreeHost(host_state_);
+  }
+
+  int setup(const pdosgpu_problem &pr, const pdosgpu_options &opt);
+  int iterate(int64_t iters, bool until_done) override;
+  int reset() override;
+  int fetch(double *x, double *s, double *y, pdosgpu_info *info) override;
+  int time_kernel(int which, int reps, double *ms) override;
+  void *stream() override { return stream_; }
+
+ private:
+  int launch_iteration();
+  int build_graph();
+  int run_prep();
+  int read_state();
+  int build_cones(const pdosgpu_problem &pr);
+
+  // sizes
+  int32_t m_ = 0, n_ = 0, nnz_ = 0, f_ = 0, l_ = 0;
+  int64_t qsize_ = 0;
+  int64_t max_iters_ = 0, cg_max_ = 0;
+  int verbose_ = 0;
+  double lambda_ = 0, alpha_ = 1, eps_ = 0, tol_sq_ = 0, pscale_ = 1, dscale_ = 1;
+
+  DeviceArena arena_;
+  cudaStream_t stream_ = nullptr;
+  cudaGraphExec_t exec_ = nullptr;
+  std::vector<cudaGraphExec_t> extra_exec_;  // [top, cg block, tail] when split
+  int cg_block_ = 0;
+  int64_t nodes_main_ = 0, nodes_top_ = 0, nodes_cg_ = 0, nodes_tail_ = 0;
+  DevState *S_ = nullptr;
+  DevState *host_state_ = nullptr;
+
+  // matrix in both layouts
+  int32_t *Rp_ = nullptr, *Rj_ = nullptr, *Ap_ = nullptr, *Ai_ = nullptr;
+  T *Rx_ = nullptr, *Ax_ = nullptr;
+  SpmvPlan<T> planA_, planT_;
+  // vectors
+  Vecs<T> V_{};
+  T *x_init_ = nullptr, *s_init_ = nullptr, *y_init_ = nullptr;
+  double *D64_ = nullptr, *E64_ = nullptr, *out_ = nullptr;
+  // reductions
+  double *partials_ = nullptr;
+  unsigned int *tickets_ = nullptr;
+  // cones
+  ConeTables ct_{};
+  int soc_grid_ = 0, socbig_grid_ = 0;
+  // grids
+  int grid_prep_ = 1, grid_top_ = 1, grid_cga_ = 1, grid_cgat_ = 1, grid_upd_ = 1, grid_post_ = 1;
+};
+
+template <typename T>
+int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
+  using namespace setup;
+  const double t0 = now_ms();
+  // ---- host-side validation (pdos.c:61-71, pdosmodule.c:94-311)
+  if (pr.n <= 0 || pr.m <= 0) return fail(PDOSGPU_EINVAL, "n and m must be positive");
+  if (!pr.Ap || !pr.b || !pr.c) return fail(PDOSGPU_EINVAL, "Ap, b and c must not be NULL");
+  const int64_t nnz64 = pr.Ap[pr.n];
+  if (nnz64 < 0) return fail(PDOSGPU_EINVAL, "Ap[n] is negative");
+  if (nnz64 > 0 && (!pr.Ai || !pr.Ax)) return fail(PDOSGPU_EINVAL, "Ai and Ax must not be NULL");
+  const int64_t lim = (int64_t)INT32_MAX - 4096;
+  if (pr.m > lim || pr.n > lim || nnz64 > lim)
+    return fail(PDOSGPU_EINVAL, "m, n and nnz must each be below 2^31 - 4096");
+  if (pr.f < 0 || pr.l < 0 || pr.qsize < 0 || (pr.qsize > 0 && !pr.q))
+    return fail(PDOSGPU_EINVAL, "cone sizes must be nonnegative");
+  int64_t rows = pr.f + pr.l;
+  for (int64_t i = 0; i < pr.qsize; ++i) {
+    if (pr.q[i] <= 0) return fail(PDOSGPU_EINVAL, "second-order cone sizes must be positive");
+    rows += pr.q[i];
+  }
+  if (rows != pr.m) return fail(PDOSGPU_EINVAL, "m does not equal f + l + sum(q)");
+  if (pr.max_iters < 0 || pr.cg_max_its < 0)
+    return fail(PDOSGPU_EINVAL, "MAX_ITERS and CG_MAX_ITS must be nonnegative");
+  if (!(pr.eps_abs >= 0) || !std::isfinite(pr.alpha) || !(pr.cg_tol >= 0))
+    return fail(PDOSGPU_EINVAL, "EPS_ABS, ALPHA and CG_TOL must be finite and nonnegative");
+
+  m_ = (int32_t)pr.m;
+  n_ = (int32_t)pr.n;
+  nnz_ = (int32_t)nnz64;
+  f_ = (int32_t)pr.f;
+  l_ = (int32_t)pr.l;
+  qsize_ = pr.qsize;
+  max_iters_ = pr.max_iters;
+  cg_max_ = pr.cg_max_its;
+  verbose_ = (int)pr.verbose;
+  alpha_ = pr.alpha;
+  eps_ = pr.eps_abs;
+  tol_sq_ = pr.cg_tol * pr.cg_tol;
+  {  // DIMACS denominators from the caller's b and c (pdos.c:76-77)
+    double sb = 0.0, sc = 0.0;
+    for (int64_t i = 0; i < pr.m; ++i) sb += pr.b[i] * pr.b[i];
+    for (int64_t i = 0; i < pr.n; ++i) sc += pr.c[i] * pr.c[i];
+    pscale_ = 1.0 + std::sqrt(sb);
+    dscale_ = 1.0 + std::sqrt(sc);
+  }
+
+  PDOS_CUDA_TRY(cudaSetDevice(opt.device));
+  g_num_sms = 0;
+  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  cudaStream_t st = stream_;
+  const int m = m_, n = n_, nnz = nnz_;
+
+  DeviceArena tmp;  // set-up temporaries
+  // ---- upload and narrow
+  int64_t *Ai64 = nullptr, *Ap64 = nullptr;
+  double *Ax0 = nullptr, *b0 = nullptr, *c0 = nullptr;
+  int *err = nullptr;
+  PDOS_TRY(tmp.alloc(&Ai64, (size_t)nnz));
+  PDOS_TRY(tmp.alloc(&Ap64, (size_t)n + 1));
+  PDOS_TRY(tmp.alloc(&Ax0, (size_t)nnz));
+  PDOS_TRY(tmp.alloc(&b0, (size_t)m));
+  PDOS_TRY(tmp.alloc(&c0, (size_t)n));
+  PDOS_TRY(tmp.alloc(&err, 1));
+  PDOS_TRY(arena_.alloc(&Ap_, (size_t)n + 1));
+  PDOS_TRY(arena_.alloc(&Ai_, (size_t)nnz + 16));
+  PDOS_TRY(arena_.alloc(&Rp_, (size_t)m + 1));
+  PDOS_TRY(arena_.alloc(&Rj_, (size_t)nnz + 16));
+  PDOS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  if (nnz > 0) {
+    PDOS_CUDA_TRY(cudaMemcpyAsync(Ai64, pr.Ai, sizeof(int64_t) * nnz, cudaMemcpyHostToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(Ax0, pr.Ax, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+  }
+  PDOS_CUDA_TRY(cudaMemcpyAsync(Ap64, pr.Ap, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(b0, pr.b, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(c0, pr.c, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  if (nnz > 0) {
+    narrow_rows_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai64, Ai_, nnz, m, err);
+    finite_check_kernel<<<grid1d(nnz), 256, 0, st>>>(Ax0, nnz, err, 4);
+  }
+  narrow_ptr_kernel<<<grid1d(n + 1), 256, 0, st>>>(Ap64, Ap_, n, nnz, err);
+  finite_check_kernel<<<grid1d(m), 256, 0, st>>>(b0, m, err, 4);
+  finite_check_kernel<<<grid1d(n), 256, 0, st>>>(c0, n, err, 4);
+  PDOS_CUDA_TRY(cudaGetLastError());
+  int herr = 0;
+  PDOS_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr & 1) return fail(PDOSGPU_EINVAL, "row index out of range in Ai");
+  if (herr & 2) return fail(PDOSGPU_EINVAL, "Ap is not a valid column pointer array");
+  if (herr & 4) return fail(PDOSGPU_EINVAL, "A, b or c holds NaN or Inf");
+
+  // ---- transpose (cs_transpose)
+  int32_t *perm = nullptr, *col_of = nullptr;
+  PDOS_TRY(tmp.alloc(&perm, (size_t)nnz));
+  PDOS_TRY(tmp.alloc(&col_of, (size_t)nnz));
+  PDOS_TRY(device_transpose(m, n, nnz, Ap_, Ai_, Rp_, perm, col_of, tmp, st));
+  if (nnz > 0) gather_col_kernel<<<grid1d(nnz), 256, 0, st>>>(perm, col_of, Rj_, nnz);
+
+  // ---- equilibration in double
+  double *Aw = nullptr, *bw = nullptr, *cw = nullptr, *xw = nullptr, *yw = nullptr, *sw = nullptr;
+  double *lam_d = nullptr;
+  PDOS_TRY(tmp.alloc(&Aw, (size_t)nnz + 16));
+  PDOS_TRY(tmp.alloc(&bw, (size_t)m));
+  PDOS_TRY(tmp.alloc(&cw, (size_t)n));
+  PDOS_TRY(tmp.alloc(&xw, (size_t)n));
+  PDOS_TRY(tmp.alloc(&yw, (size_t)m));
+  PDOS_TRY(tmp.alloc(&sw, (size_t)m));
+  PDOS_TRY(tmp.alloc(&lam_d, 1));
+  PDOS_TRY(arena_.alloc(&D64_, (size_t)m));
+  PDOS_TRY(arena_.alloc(&E64_, (size_t)n));
+  PDOS_CUDA_TRY(cudaMemsetAsync(xw, 0, sizeof(double) * n, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(yw, 0, sizeof(double) * m, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(sw, 0, sizeof(double) * m, st));
+  if (pr.x0) PDOS_CUDA_TRY(cudaMemcpyAsync(xw, pr.x0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  if (pr.y0) PDOS_CUDA_TRY(cudaMemcpyAsync(yw, pr.y0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  if (pr.s0) PDOS_CUDA_TRY(cudaMemcpyAsync(sw, pr.s0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+
+  // cone row tables (host -> device)
+  const int32_t soc0 = f_ + l_;
+  std::vector<int32_t> cone_of_row_h;
+  std::vector<int64_t> cone_off_h(qsize_), cone_len_h(qsize_);
+  int32_t *cone_of_row = nullptr;
+  int64_t *cone_off = nullptr, *cone_len = nullptr;
+  if (qsize_ > 0) {
+    cone_of_row_h.assign(m, -1);
+    int64_t off = soc0;
+    for (int64_t c = 0; c < qsize_; ++c) {
+      cone_off_h[c] = off;
+      cone_len_h[c] = pr.q[c];
+      for (int64_t i = 0; i < pr.q[c]; ++i) cone_of_row_h[off + i] = (int32_t)c;
+      off += pr.q[c];
+    }
+    PDOS_TRY(tmp.alloc(&cone_of_row, (size_t)m));
+    PDOS_TRY(tmp.alloc(&cone_off, (size_t)qsize_));
+    PDOS_TRY(tmp.alloc(&cone_len, (size_t)qsize_));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_of_row, cone_of_row_h.data(), sizeof(int32_t) * m,
+                                  cudaMemcpyHostToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_off, cone_off_h.data(), sizeof(int64_t) * qsize_,
+                                  cudaMemcpyHostToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_len, cone_len_h.data(), sizeof(int64_t) * qsize_,
+                                  cudaMemcpyHostToDevice, st));
+  }
+
+  const bool ruiz = pr.normalize && opt.scaling == PDOSGPU_SCALE_RUIZ;
+  if (!pr.normalize) {
+    fill_kernel<<<grid1d(m), 256, 0, st>>>(D64_, m, 1.0);
+    fill_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1.0);
+    if (nnz > 0) PDOS_CUDA_TRY(cudaMemcpyAsync(Aw, Ax0, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st));
+  } else if (!ruiz) {
+    // common.h:69-137
+    double *Rx0 = nullptr;
+    PDOS_TRY(tmp.alloc(&Rx0, (size_t)nnz));
+    if (nnz > 0) gather_kernel<double><<<grid1d(nnz), 256, 0, st>>>(perm, Ax0, Rx0, nnz);
+    row_sumsq_kernel<<<grid1d(m, 128), 128, 0, st>>>(Rp_, Rx0, m, D64_);
+    if (qsize_ > 0) {
+      double *mean = nullptr;
+      PDOS_TRY(tmp.alloc(&mean, (size_t)qsize_));
+      cone_mean_kernel<<<grid1d(qsize_, 128), 128, 0, st>>>(D64_, cone_off, cone_len, (int)qsize_, mean);
+      cone_broadcast_kernel<<<grid1d(m - soc0), 256, 0, st>>>(D64_, cone_of_row, mean, soc0, m);
+    }
+    clamp_rsqrt_kernel<<<grid1d(m), 256, 0, st>>>(D64_, m);
+    if (nnz > 0) {
+      PDOS_CUDA_TRY(cudaMemcpyAsync(Aw, Ax0, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st));
+      scale_by_row_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, Ai_, D64_, nnz);
+    }
+    col_sumsq_kernel<<<grid1d(n, 128), 128, 0, st>>>(Ap_, Aw, n, E64_);
+    clamp_rsqrt_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n);
+    if (nnz > 0) scale_by_col_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, col_of, E64_, nnz);
+  } else {
+    // ruiz_equil_common.h:130-245
+    double *cv = nullptr, *cb = nullptr, *rowmax = nullptr, *colmax = nullptr, *sc = nullptr;
+    int32_t *ci = nullptr;
+    PDOS_TRY(tmp.alloc(&cv, (size_t)nnz));
+    PDOS_TRY(tmp.alloc(&ci, (size_t)nnz));
+    PDOS_TRY(tmp.alloc(&cb, (size_t)m));
+    PDOS_TRY(tmp.alloc(&rowmax, (size_t)m));
+    PDOS_TRY(tmp.alloc(&colmax, (size_t)n));
+    PDOS_TRY(tmp.alloc(&sc, 4));
+    if (qsize_ > 0) {
+      int *head = nullptr, *run_excl = nullptr;
+      PDOS_TRY(tmp.alloc(&head, (size_t)nnz));
+      PDOS_TRY(tmp.alloc(&run_excl, (size_t)nnz + 1));
+      if (nnz > 0) run_heads_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai_, cone_of_row, nnz, head);
+      PDOS_TRY(device_excl_scan(head, nnz, run_excl, true, tmp, st));
+      int nruns = 0;
+      PDOS_CUDA_TRY(cudaMemcpyAsync(&nruns, run_excl + nnz, sizeof(int), cudaMemcpyDeviceToHost, st));
+      PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+      double *runmax = nullptr;
+      PDOS_TRY(tmp.alloc(&runmax, (size_t)nruns));
+      PDOS_CUDA_TRY(cudaMemsetAsync(runmax, 0, sizeof(double) * (nruns > 0 ? nruns : 1), st));
+      if (nnz > 0) {
+        run_max_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai_, cone_of_row, Ax0, run_excl, head, nnz, runmax);
+        run_apply_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai_, cone_of_row, cone_off, Ax0, run_excl, head,
+                                                      runmax, nnz, cv, ci);
+      }
+      double *cmax = nullptr;
+      PDOS_TRY(tmp.alloc(&cmax, (size_t)qsize_));
+      PDOS_CUDA_TRY(cudaMemsetAsync(cmax, 0, sizeof(double) * qsize_, st));
+      cone_absmax_kernel<<<grid1d(m - soc0), 256, 0, st>>>(b0, cone_of_row, soc0, m, cmax);
+      cone_collapse_b_kernel<<<grid1d(m), 256, 0, st>>>(b0, cone_of_row, cmax, m, cb);
+    } else {
+      if (nnz > 0) {
+        PDOS_CUDA_TRY(cudaMemcpyAsync(cv, Ax0, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st));
+        PDOS_CUDA_TRY(cudaMemcpyAsync(ci, Ai_, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, st));
+      }
+      PDOS_CUDA_TRY(cudaMemcpyAsync(cb, b0, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+    }
+    fill_kernel<<<grid1d(m), 256, 0, st>>>(D64_, m, 1.0);
+    fill_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1.0);
+    PDOS_CUDA_TRY(cudaMemsetAsync(rowmax, 0, sizeof(double) * m, st));
+    PDOS_CUDA_TRY(cudaMemsetAsync(colmax, 0, sizeof(double) * n, st));
+    const double sc_init[4] = {1.0, 1.0, 0.0, 0.0};
+    PDOS_CUDA_TRY(cudaMemcpyAsync(sc, sc_init, sizeof(sc_init), cudaMemcpyHostToDevice, st));
+    for (int pass = 0; pass < 3; ++pass) {
+      if (nnz > 0) ruiz_rowmax_kernel<<<grid1d(nnz), 256, 0, st>>>(cv, ci, col_of, E64_, nnz, rowmax);
+      ruiz_lastpi_kernel<<<grid1d(n), 256, 0, st>>>(c0, E64_, n, sc);
+      ruiz_row_finish_kernel<<<grid1d(m), 256, 0, st>>>(cb, sc, m, rowmax);
+      if (qsize_ > 0)
+        ruiz_cone_rows_kernel<<<grid1d(m - soc0), 256, 0, st>>>(cone_of_row, cone_off, soc0, m, rowmax);
+      ruiz_update_kernel<<<grid1d(m), 256, 0, st>>>(D64_, rowmax, m);
+      ruiz_last_kernel<<<1, 32, 0, st>>>(sc, 0);
+      ruiz_colmax_kernel<<<grid1d(n, 128), 128, 0, st>>>(Ap_, cv, ci, D64_, c0, sc, n, colmax);
+      ruiz_lastdelta_kernel<<<grid1d(m), 256, 0, st>>>(cb, D64_, m, sc);
+      ruiz_update_kernel<<<grid1d(n), 256, 0, st>>>(E64_, colmax, n);
+      ruiz_last_kernel<<<1, 32, 0, st>>>(sc, 1);
+    }
+    if (nnz > 0) ruiz_scale_kernel<<<grid1d(nnz), 256, 0, st>>>(Ax0, Ai_, col_of, D64_, E64_, nnz, Aw);
+  }
+  // c, b and the warm start (common.h:139-161); lambda (common.h:182);
+  // x-space ratio (common.h:185-192)
+  if (pr.normalize) {
+    vec_scale_kernel<<<grid1d(n), 256, 0, st>>>(c0, E64_, cw, n, 0);
+    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(b0, D64_, bw, m, 0);
+    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(yw, D64_, yw, m, 1);
+    vec_scale_kernel<<<grid1d(n), 256, 0, st>>>(xw, E64_, xw, n, 1);
+    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(sw, D64_, sw, m, 0);
+  } else {
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cw, c0, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(bw, b0, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+  }
+  lambda_kernel<<<1, 32, 0, st>>>(bw, m, cw, n, ruiz ? 1e-6 : 1e-15, lam_d);
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1e3, 0);
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(cw, n, 1e3, 0);
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(xw, n, 1e3, 1);
+  if (nnz > 0) scal_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, nnz, 1e3, 0);
+  PDOS_CUDA_TRY(cudaMemcpyAsync(&lambda_, lam_d, sizeof(double), cudaMemcpyDeviceToHost, st));
+  PDOS_CUDA_TRY(cudaGetLastError());
+
+  // ---- working arrays in T
+  PDOS_TRY(arena_.alloc(&Ax_, (size_t)nnz + 16));
+  PDOS_TRY(arena_.alloc(&Rx_, (size_t)nnz + 16));
+  T *bT, *cT, *DT, *ET;
+  PDOS_TRY(arena_.alloc(&bT, (size_t)m));
+  PDOS_TRY(arena_.alloc(&cT, (size_t)n));
+  PDOS_TRY(arena_.alloc(&DT, (size_t)m));
+  PDOS_TRY(arena_.alloc(&ET, (size_t)n));
+  if (nnz > 0) {
+    double *Rxd = nullptr;
+    PDOS_TRY(tmp.alloc(&Rxd, (size_t)nnz));
+    gather_kernel<double><<<grid1d(nnz), 256, 0, st>>>(perm, Aw, Rxd, nnz);
+    convert_kernel<T><<<grid1d(nnz), 256, 0, st>>>(Aw, Ax_, nnz);
+    convert_kernel<T><<<grid1d(nnz), 256, 0, st>>>(Rxd, Rx_, nnz);
+  }
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(bw, bT, m);
+  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(cw, cT, n);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(D64_, DT, m);
+  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(E64_, ET, n);
+  PDOS_TRY(arena_.alloc(&x_init_, (size_t)n));
+  PDOS_TRY(arena_.alloc(&y_init_, (size_t)m));
+  PDOS_TRY(arena_.alloc(&s_init_, (size_t)m));
+  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(xw, x_init_, n);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(yw, y_init_, m);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(sw, s_init_, m);
+
+  V_.m = m;
+  V_.n = n;
+  V_.f = f_;
+  V_.l = l_;
+  V_.b = bT;
+  V_.c = cT;
+  V_.D = DT;
+  V_.E = ET;
+  PDOS_TRY(arena_.alloc(&V_.x, (size_t)n));
+  PDOS_TRY(arena_.alloc(&V_.p, (size_t)n));
+  PDOS_TRY(arena_.alloc(&V_.q, (size_t)n));
+  PDOS_TRY(arena_.alloc(&V_.t, (size_t)n));
+  PDOS_TRY(arena_.alloc(&V_.s, (size_t)m));
+  PDOS_TRY(arena_.alloc(&V_.y, (size_t)m));
+  PDOS_TRY(arena_.alloc(&V_.st, (size_t)m));
+  PDOS_TRY(arena_.alloc(&V_.u, (size_t)m));
+  PDOS_TRY(arena_.alloc(&V_.ax, (size_t)m));
+  PDOS_TRY(arena_.alloc(&out_, (size_t)n + 2 * (size_t)m));
+  PDOS_CUDA_TRY(cudaGetLastError());
+
+  // ---- tiles (host, from the two pointer arrays)
+  {
+    std::vector<int32_t> rp(m + 1), ap(n + 1);
+    PDOS_CUDA_TRY(cudaMemcpyAsync(rp.data(), Rp_, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, st));
+    PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int64_t j = 0; j <= n; ++j) ap[j] = (int32_t)pr.Ap[j];
+    SpmvPlan<T> *plans[2] = {&planA_, &planT_};
+    const std::vector<int32_t> *ptrs[2] = {&rp, &ap};
+    const int rows_of[2] = {m, n};
+    for (int k = 0; k < 2; ++k) {
+      SpmvPlan<T> &pl = *plans[k];
+      build_tiles(ptrs[k]->data(), rows_of[k], kTileNnz, kMaxTileRows, pl.tiles_h, pl.longs_h, pl.slots);
+      PDOS_TRY(arena_.alloc(&pl.tiles, pl.tiles_h.size()));
+      PDOS_TRY(arena_.alloc(&pl.longs, pl.longs_h.size()));
+      PDOS_TRY(arena_.alloc(&pl.chunk_partial, (size_t)pl.slots * 2 + 2));
+      PDOS_TRY(arena_.alloc(&pl.long_ticket, pl.longs_h.size() + 1));
+      if (!pl.tiles_h.empty())
+        PDOS_CUDA_TRY(cudaMemcpyAsync(pl.tiles, pl.tiles_h.data(), sizeof(Tile) * pl.tiles_h.size(),
+                                      cudaMemcpyHostToDevice, st));
+      if (!pl.longs_h.empty())
+        PDOS_CUDA_TRY(cudaMemcpyAsync(pl.longs, pl.longs_h.data(), sizeof(LongRow) * pl.longs_h.size(),
+                                      cudaMemcpyHostToDevice, st));
+      PDOS_CUDA_TRY(cudaMemsetAsync(pl.long_ticket, 0, sizeof(unsigned) * (pl.longs_h.size() + 1), st));
+    }
+  }
+  PDOS_TRY(build_cones(pr));
+
+  // ---- grids and reduction scratch
+  const int tA = (int)planA_.tiles_h.size(), tT = (int)planT_.tiles_h.size();
+  grid_prep_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpPrep<T>>, kBlock,
+                               sizeof(T) * kTileNnz, std::max(tA, 1));
+  grid_top_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpTop<T>>, kBlock,
+                              sizeof(T) * kTileNnz * 2, std::max(tT, 1));
+  grid_cga_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpCgA<T>>, kBlock,
+                              sizeof(T) * kTileNnz, std::max(tA, 1));
+  grid_cgat_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpCgAt<T>>, kBlock,
+                               sizeof(T) * kTileNnz, std::max(tT, 1));
+  grid_post_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpPost<T>>, kBlock,
+                               sizeof(T) * kTileNnz, std::max(tA, 1));
+  grid_upd_ = persistent_grid(cg_update_kernel<T, kBlock>, kBlock, 0, (n + kBlock - 1) / kBlock);
+  size_t slots = 0;
+  slots = std::max(slots, (size_t)grid_prep_ * 2);
+  slots = std::max(slots, (size_t)grid_top_ * 3);
+  slots = std::max(slots, (size_t)grid_cgat_);
+  slots = std::max(slots, (size_t)grid_upd_);
+  slots = std::max(slots, (size_t)(grid_post_ + soc_grid_ + socbig_grid_) * 2);
+  PDOS_TRY(arena_.alloc(&partials_, slots));
+  PDOS_TRY(arena_.alloc(&tickets_, 8));
+  PDOS_CUDA_TRY(cudaMemsetAsync(tickets_, 0, sizeof(unsigned) * 8, st));
+
+  // ---- state
+  PDOS_TRY(arena_.alloc(&S_, 1));
+  PDOS_CUDA_TRY(cudaMallocHost(&host_state_, sizeof(DevState)));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  tmp.release();
+  PDOS_TRY(reset());
+  PDOS_TRY(build_graph());
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  setup_ms = now_ms() - t0;
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::build_cones(const pdosgpu_problem &pr) {
+  cudaStream_t st = stream_;
+  std::vector<int32_t> small_off, small_len, chunk_row0, chunk_row1, chunk_cone, big_head, big_chunk0,
+      big_nchunks;
+  int64_t off = (int64_t)f_ + l_;
+  for (int64_t c = 0; c < qsize_; ++c) {
+    const int64_t q = pr.q[c];
+    if (q <= kSmallCone) {
+      small_off.push_back((int32_t)off);
+      small_len.push_back((int32_t)q);
+    } else {
+      const int32_t big = (int32_t)big_head.size();
+      big_head.push_back((int32_t)off);
+      big_chunk0.push_back((int32_t)chunk_row0.size());
+      int32_t nch = 0;
+      for (int64_t r = off; r < off + q; r += kConeChunk) {
+        chunk_row0.push_back((int32_t)r);
+        chunk_row1.push_back((int32_t)std::min<int64_t>(off + q, r + kConeChunk));
+        chunk_cone.push_back(big);
+        ++nch;
+      }
+      big_nchunks.push_back(nch);
+    }
+    off += q;
+  }
+  auto up = [&](const std::vector<int32_t> &v, const int32_t **dst) -> int {
+    int32_t *p = nullptr;
+    PDOS_TRY(arena_.alloc(&p, v.size() + 1));
+    if (!v.empty())
+      PDOS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, st));
+    *dst = p;
+    return PDOSGPU_OK;
+  };
+  PDOS_TRY(up(small_off, &ct_.small_off));
+  PDOS_TRY(up(small_len, &ct_.small_len));
+  PDOS_TRY(up(chunk_row0, &ct_.chunk_row0));
+  PDOS_TRY(up(chunk_row1, &ct_.chunk_row1));
+  PDOS_TRY(up(chunk_cone, &ct_.chunk_cone));
+  PDOS_TRY(up(big_head, &ct_.big_head));
+  PDOS_TRY(up(big_chunk0, &ct_.big_chunk0));
+  PDOS_TRY(up(big_nchunks, &ct_.big_nchunks));
+  ct_.n_small = (int32_t)small_off.size();
+  ct_.n_chunks = (int32_t)chunk_row0.size();
+  PDOS_TRY(arena_.alloc(&ct_.chunk_sq, chunk_row0.size() + 1));
+  PDOS_TRY(arena_.alloc(&ct_.big_headval, big_head.size() + 1));
+  const int warps = kBlock / 32;
+  ct_.small_blocks = ct_.n_small > 0 ? std::min((ct_.n_small + warps - 1) / warps, num_sms() * 8) : 0;
+  soc_grid_ = qsize_ > 0 ? ct_.small_blocks + ct_.n_chunks : 0;
+  socbig_grid_ = ct_.n_chunks;
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::run_prep() {
+  GridReduce gr{partials_, tickets_ + 0, 0, grid_prep_, 1};
+  OpPrep<T> op{V_, (T)lambda_, S_};
+  spmv_kernel<T, kBlock, kTileNnz, OpPrep<T>>
+      <<<grid_prep_, kBlock, sizeof(T) * kTileNnz, stream_>>>(
+          CsrDev<T>{Rp_, Rj_, Rx_, m_}, planA_.view(), op, gr);
+  PDOS_CUDA_TRY(cudaGetLastError());
+  launches += 1;
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::reset() {
+  cudaStream_t st = stream_;
+  DevState h{};
+  h.lambda = lambda_;
+  h.alpha_relax = alpha_;
+  h.eps = eps_;
+  h.pscale = pscale_;
+  h.dscale = dscale_;
+  h.tol_sq = tol_sq_;
+  h.max_iters = max_iters_;
+  h.cg_max = cg_max_;
+  h.p_res = h.d_res = h.p_obj = h.d_obj = h.eta = -1.0;
+  h.done = max_iters_ <= 0 ? 1 : 0;
+  *host_state_ = h;
+  PDOS_CUDA_TRY(cudaMemcpyAsync(S_, host_state_, sizeof(DevState), cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(V_.x, x_init_, sizeof(T) * n_, cudaMemcpyDeviceToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(V_.y, y_init_, sizeof(T) * m_, cudaMemcpyDeviceToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(V_.s, s_init_, sizeof(T) * m_, cudaMemcpyDeviceToDevice, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(V_.p, 0, sizeof(T) * n_, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(V_.q, 0, sizeof(T) * n_, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(V_.t, 0, sizeof(T) * n_, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(V_.st, 0, sizeof(T) * m_, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(V_.u, 0, sizeof(T) * m_, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(V_.ax, 0, sizeof(T) * m_, st));
+  PDOS_TRY(run_prep());
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::build_graph() {
+  cudaStream_t st = stream_;
+  const CsrDev<T> A{Rp_, Rj_, Rx_, m_};
+  const CsrDev<T> At{Ap_, Ai_, Ax_, n_};
+  const T lam = (T)lambda_;
+  auto top = [&]() {
+    GridReduce gr{partials_, tickets_ + 1, 0, grid_top_, 1};
+    spmv_kernel<T, kBlock, kTileNnz, OpTop<T>><<<grid_top_, kBlock, sizeof(T) * kTileNnz * 2, st>>>(
+        At, planT_.view(), OpTop<T>{V_, lam, S_}, gr);
+  };
+  auto cg = [&]() {
+    GridReduce none{partials_, tickets_ + 2, 0, grid_cga_, 0};
+    spmv_kernel<T, kBlock, kTileNnz, OpCgA<T>><<<grid_cga_, kBlock, sizeof(T) * kTileNnz, st>>>(
+        A, planA_.view(), OpCgA<T>{V_, S_}, none);
+    GridReduce g2{partials_, tickets_ + 3, 0, grid_cgat_, 1};
+    spmv_kernel<T, kBlock, kTileNnz, OpCgAt<T>><<<grid_cgat_, kBlock, sizeof(T) * kTileNnz, st>>>(
+        At, planT_.view(), OpCgAt<T>{V_, S_}, g2);
+    GridReduce g3{partials_, tickets_ + 4, 0, grid_upd_, 1};
+    cg_update_kernel<T, kBlock><<<grid_upd_, kBlock, 0, st>>>(V_, S_, g3);
+  };
+  auto tail = [&]() {
+    const int total = grid_post_ + soc_grid_ + socbig_grid_;
+    GridReduce g5{partials_, tickets_ + 5, 0, total, qsize_ == 0 ? 1 : 0};
+    OpPost<T> op{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_};
+    spmv_kernel<T, kBlock, kTileNnz, OpPost<T>><<<grid_post_, kBlock, sizeof(T) * kTileNnz, st>>>(
+        A, planA_.view(), op, g5);
+    if (qsize_ > 0) {
+      GridReduce g6{partials_, tickets_ + 6, grid_post_, total, socbig_grid_ == 0 ? 1 : 0};
+      soc_kernel<T, kBlock><<<soc_grid_, kBlock, 0, st>>>(V_, ct_, lam, S_, g6);
+      if (socbig_grid_ > 0) {
+        GridReduce g7{partials_, tickets_ + 7, grid_post_ + soc_grid_, total, 1};
+        soc_big_kernel<T, kBlock><<<socbig_grid_, kBlock, 0, st>>>(V_, ct_, lam, S_, g7);
+      }
+    }
+  };
+  int64_t last_nodes = 0;
+  auto capture = [&](auto &&body, cudaGraphExec_t *exec) -> int {
+    cudaGraph_t graph = nullptr;
+    PDOS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return fail(PDOSGPU_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    size_t nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, &nodes);
+    last_nodes = (int64_t)nodes;
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(PDOSGPU_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    return PDOSGPU_OK;
+  };
+  if (cg_max_ <= 64) {
+    PDOS_TRY(capture(
+        [&]() {
+          top();
+          for (int64_t k = 0; k < cg_max_; ++k) cg();
+          tail();
+        },
+        &exec_));
+    nodes_main_ = last_nodes;
+  } else {
+    cg_block_ = 16;
+    extra_exec_.assign(3, nullptr);
+    PDOS_TRY(capture([&]() { top(); }, &extra_exec_[0]));
+    nodes_top_ = last_nodes;
+    PDOS_TRY(capture(
+        [&]() {
+          for (int k = 0; k < cg_block_; ++k) cg();
+        },
+        &extra_exec_[1]));
+    nodes_cg_ = last_nodes;
+    PDOS_TRY(capture([&]() { tail(); }, &extra_exec_[2]));
+    nodes_tail_ = last_nodes;
+  }
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::launch_iteration() {
+  if (exec_) {
+    PDOS_CUDA_TRY(cudaGraphLaunch(exec_, stream_));
+    launches += nodes_main_;
+  } else {
+    PDOS_CUDA_TRY(cudaGraphLaunch(extra_exec_[0], stream_));
+    for (int64_t k = 0; k < cg_max_; k += cg_block_) {
+      PDOS_CUDA_TRY(cudaGraphLaunch(extra_exec_[1], stream_));
+      launches += nodes_cg_;
+    }
+    PDOS_CUDA_TRY(cudaGraphLaunch(extra_exec_[2], stream_));
+    launches += nodes_top_ + nodes_tail_;
+  }
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::read_state() {
+  PDOS_CUDA_TRY(cudaMemcpyAsync(host_state_, S_, sizeof(DevState), cudaMemcpyDeviceToHost, stream_));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(stream_));
+  return PDOSGPU_OK;
+}
+
+static void print_header() {
+  printf(" iter |  ||Ax+s-b||    ||A'y+c||       c'x          -b'y          eta    \n");
+  printf("==========================================================================\n");
+}
+
+static void print_row(long long i, const DevState &s) {
+  printf("%5lld | %11.3e   %10.3e   %11.3e   %11.3e   %10.3e   \n", i, s.p_res, s.d_res, s.p_obj,
+         s.d_obj, s.eta);
+}
+
+template <typename T>
+int Engine<T>::iterate(int64_t iters, bool until_done) {
+  const double t0 = now_ms();
+  PDOS_TRY(read_state());
+  if (host_state_->done || iters <= 0) {
+    solve_ms = now_ms() - t0;
+    return PDOSGPU_OK;
+  }
+  if (verbose_) {
+    printf("lambda: %5.3e\n\n", lambda_);
+    print_header();
+    int64_t done_iters = 0;
+    while (done_iters < iters) {
+      const long long before = host_state_->admm_iter;
+      PDOS_TRY(launch_iteration());
+      PDOS_TRY(read_state());
+      ++done_iters;
+      const DevState &s = *host_state_;
+      if (s.solved || s.done) {
+        print_row(s.solved ? before : s.admm_iter, s);
+        break;
+      }
+      if (before % 10 == 0) print_row(before, s);
+    }
+    printf("Total solve time is %4.8fs\n", (now_ms() - t0) / 1e3);
+  } else {
+    int64_t launched = 0;
+    int64_t batch = 1;
+    while (launched < iters) {
+      const int64_t nb = std::min<int64_t>(batch, iters - launched);
+      for (int64_t i = 0; i < nb; ++i) PDOS_TRY(launch_iteration());
+      launched += nb;
+      if (until_done || launched >= iters) {
+        PDOS_TRY(read_state());
+        if (host_state_->done) break;
+      }
+      if (batch < 16) batch *= 2;
+    }
+  }
+  PDOS_TRY(read_state());
+  solve_ms = now_ms() - t0;
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+__global__ void unscale_kernel(const T *x, const T *s, const T *y, const double *D, const double *E,
+                               int n, int m, double *out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n + m; i += gridDim.x * blockDim.x) {
+    if (i < n) {
+      out[i] = E[i] * (double)x[i];  // pdos.c:272-282
+    } else {
+      const int r = i - n;
+      out[n + r] = (double)s[r] / D[r];      // pdos.c:284-294
+      out[n + m + r] = D[r] * (double)y[r];  // pdos.c:261-270
+    }
+  }
+}
+
+template <typename T>
+int Engine<T>::fetch(double *x, double *s, double *y, pdosgpu_info *info) {
+  cudaStream_t st = stream_;
+  unscale_kernel<T><<<grid1d(n_ + m_), 256, 0, st>>>(V_.x, V_.s, V_.y, D64_, E64_, n_, m_, out_);
+  PDOS_CUDA_TRY(cudaGetLastError());
+  if (x) PDOS_CUDA_TRY(cudaMemcpyAsync(x, out_, sizeof(double) * n_, cudaMemcpyDeviceToHost, st));
+  if (s) PDOS_CUDA_TRY(cudaMemcpyAsync(s, out_ + n_, sizeof(double) * m_, cudaMemcpyDeviceToHost, st));
+  if (y) PDOS_CUDA_TRY(cudaMemcpyAsync(y, out_ + n_ + m_, sizeof(double) * m_, cudaMemcpyDeviceToHost, st));
+  PDOS_TRY(read_state());
+  if (info) {
+    const DevState &h = *host_state_;
+    info->admm_iters = h.admm_iter;
+    info->cg_iters = h.cg_total;
+    info->solved = h.solved;
+    info->p_res = h.p_res;
+    info->d_res = h.d_res;
+    info->p_obj = h.p_obj;
+    info->d_obj = h.d_obj;
+    info->eta = h.eta;
+    info->lambda = lambda_;
+    info->setup_ms = setup_ms;
+    info->solve_ms = solve_ms;
+    info->kernel_launches = launches;
+  }
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int Engine<T>::time_kernel(int which, int reps, double *ms) {
+  if (reps <= 0 || !ms) return fail(PDOSGPU_EINVAL, "reps must be positive");
+  cudaStream_t st = stream_;
+  // make every kernel do its full work: not done, CG active, lazy update on
+  PDOS_TRY(read_state());
+  DevState h = *host_state_;
+  h.done = 0;
+  h.cg_active = 1;
+  h.p_lazy = 1;
+  h.ratio = 0.5;
+  h.qsold = 1.0;
+  h.cg_iter = 0;
+  h.max_iters = INT64_MAX / 2;
+  *host_state_ = h;
+  PDOS_CUDA_TRY(cudaMemcpyAsync(S_, host_state_, sizeof(DevState), cudaMemcpyHostToDevice, st));
+  const CsrDev<T> A{Rp_, Rj_, Rx_, m_};
+  const CsrDev<T> At{Ap_, Ai_, Ax_, n_};
+  const T lam = (T)lambda_;
+  cudaEvent_t e0, e1;
+  PDOS_CUDA_TRY(cudaEventCreate(&e0));
+  PDOS_CUDA_TRY(cudaEventCreate(&e1));
+  auto launch = [&]() {
+    switch (which) {
+      case 0: {
+        GridReduce none{partials_, tickets_ + 2, 0, grid_cga_, 0};
+        spmv_kernel<T, kBlock, kTileNnz, OpCgA<T>><<<grid_cga_, kBlock, sizeof(T) * kTileNnz, st>>>(
+            A, planA_.view(), OpCgA<T>{V_, S_}, none);
+        break;
+      }
+      case 1: {
+        GridReduce g2{partials_, tickets_ + 3, 0, grid_cgat_, 1};
+        spmv_kernel<T, kBlock, kTileNnz, OpCgAt<T>><<<grid_cgat_, kBlock, sizeof(T) * kTileNnz, st>>>(
+            At, planT_.view(), OpCgAt<T>{V_, S_}, g2);
+        break;
+      }
+      case 2: {
+        GridReduce gr{partials_, tickets_ + 1, 0, grid_top_, 0};
+        spmv_kernel<T, kBlock, kTileNnz, OpTop<T>><<<grid_top_, kBlock, sizeof(T) * kTileNnz * 2, st>>>(
+            At, planT_.view(), OpTop<T>{V_, lam, S_}, gr);
+        break;
+      }
+      default: {
+        GridReduce g5{partials_, tickets_ + 5, 0, grid_post_, 0};
+        OpPost<T> op{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_};
+        spmv_kernel<T, kBlock, kTileNnz, OpPost<T>><<<grid_post_, kBlock, sizeof(T) * kTileNnz, st>>>(
+            A, planA_.view(), op, g5);
+      }
+    }
+  };
+  launch();  // warm-up
+  PDOS_CUDA_TRY(cudaEventRecord(e0, st));
+  for (int r = 0; r < reps; ++r) launch();
+  PDOS_CUDA_TRY(cudaEventRecord(e1, st));
+  PDOS_CUDA_TRY(cudaGetLastError());
+  PDOS_CUDA_TRY(cudaEventSynchronize(e1));
+  float total = 0.f;
+  PDOS_CUDA_TRY(cudaEventElapsedTime(&total, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  launches += reps + 1;
+  *ms = (double)total / reps;
+  return PDOSGPU_OK;
+}
+
+int make_engine(const pdosgpu_problem &prob, const pdosgpu_options &opt,
+                std::unique_ptr<EngineBase> &out) {
+  if (opt.precision == PDOSGPU_FP32) {
+    auto e = std::make_unique<Engine<float>>();
+    PDOS_TRY(e->setup(prob, opt));
+    out = std::move(e);
+  } else if (opt.precision == PDOSGPU_FP64) {
+    auto e = std::make_unique<Engine<double>>();
+    PDOS_TRY(e->setup(prob, opt));
+    out = std::move(e);
+  } else {
+    return fail(PDOSGPU_EINVAL, "unknown precision");
+  }
+  return PDOSGPU_OK;
+}
+
+}  // namespace pdosgpu

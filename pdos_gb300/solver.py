@@ -1,0 +1,250 @@
+"""Python front end of the GPU solver.
+
+* ``solve(c, A, b, dims, opts, x0, y0, s0)`` mirrors the reference's Python
+  binding (pdosmodule.c:27-344): same arguments, defaults (pdosmodule.c:66-74),
+  validation messages and result dict ('x', 's', 'y', 'status'), on numpy /
+  scipy inputs instead of CVXOPT matrices.
+* ``Workspace`` exposes the C-ABI life cycle (setup / solve / iterate /
+  reset / fetch) for callers that keep a problem resident on the GPU.
+* ``pdos_call`` goes through the reference-compatible ``pdos()`` entry point.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .abi import Marshalled, read_sol
+from .problem import DEFAULT_PARAMS, Problem
+
+_PRECISION = {"fp64": _lib.PDOSGPU_FP64, "fp32": _lib.PDOSGPU_FP32}
+_SCALING = {"2norm": _lib.PDOSGPU_SCALE_2NORM, "ruiz": _lib.PDOSGPU_SCALE_RUIZ}
+
+
+def make_options(precision="fp64", scaling="2norm", device=0):
+    if precision not in _PRECISION:
+        raise ValueError(f"precision must be one of {sorted(_PRECISION)}")
+    if scaling not in _SCALING:
+        raise ValueError(f"scaling must be one of {sorted(_SCALING)}")
+    opt = _lib.Options()
+    _lib.load().pdosgpu_default_options(ctypes.byref(opt))
+    opt.precision = _PRECISION[precision]
+    opt.scaling = _SCALING[scaling]
+    opt.device = device
+    return opt
+
+
+class Workspace:
+    """A problem resident on the GPU (pdosgpu_setup ... pdosgpu_free)."""
+
+    def __init__(self, prob, precision="fp64", scaling="2norm", device=0):
+        self.lib = _lib.load()
+        self.prob = prob
+        self._keep = []
+
+        def f64(a):
+            if a is None:
+                return ctypes.POINTER(ctypes.c_double)()
+            a = np.ascontiguousarray(a, np.float64)
+            self._keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+        def i64(a):
+            a = np.ascontiguousarray(a, np.int64)
+            self._keep.append(a)
+            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+        p = prob.params
+        q = np.asarray(prob.q, np.int64) if len(prob.q) else np.zeros(1, np.int64)
+        self._c_prob = _lib.Problem(
+            prob.n, prob.m, f64(prob.Ax), i64(prob.Ai), i64(prob.Ap), f64(prob.b), f64(prob.c),
+            f64(prob.x0), f64(prob.y0), f64(prob.s0), prob.f, prob.l, len(prob.q), i64(q),
+            int(p["MAX_ITERS"]), int(p["CG_MAX_ITS"]), float(p["EPS_ABS"]), float(p["ALPHA"]),
+            float(p["CG_TOL"]), int(p["VERBOSE"]), int(p["NORMALIZE"]))
+        self._opt = make_options(precision, scaling, device)
+        self._w = ctypes.c_void_p()
+        _lib.check(self.lib.pdosgpu_setup(ctypes.byref(self._c_prob), ctypes.byref(self._opt),
+                                          ctypes.byref(self._w)), "pdosgpu_setup", self.lib)
+
+    def solve(self):
+        _lib.check(self.lib.pdosgpu_solve(self._w), "pdosgpu_solve", self.lib)
+        return self
+
+    def iterate(self, iters):
+        _lib.check(self.lib.pdosgpu_iterate(self._w, int(iters)), "pdosgpu_iterate", self.lib)
+        return self
+
+    def reset(self):
+        _lib.check(self.lib.pdosgpu_reset(self._w), "pdosgpu_reset", self.lib)
+        return self
+
+    def fetch(self):
+        n, m = self.prob.n, self.prob.m
+        x, s, y = np.zeros(n), np.zeros(m), np.zeros(m)
+        info = _lib.Info()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _lib.check(self.lib.pdosgpu_fetch(self._w, x.ctypes.data_as(dp), s.ctypes.data_as(dp),
+                                          y.ctypes.data_as(dp), ctypes.byref(info)),
+                   "pdosgpu_fetch", self.lib)
+        d = info.as_dict()
+        d["lambda"] = d.pop("lambda_")
+        return {"x": x, "s": s, "y": y,
+                "status": "Solved" if info.solved else "Indeterminate",
+                "iters": info.admm_iters, "cg_iters": info.cg_iters, "info": d}
+
+    @property
+    def stream(self):
+        """cudaStream_t (as an int) that the workspace's kernels run on."""
+        return self.lib.pdosgpu_stream(self._w)
+
+    def time_kernel(self, which, reps=20):
+        """Mean ms per launch of one SpMV kernel (0: CG A, 1: CG A', 2: top
+        A', 3: post A); the iterate must be reset afterwards."""
+        ms = ctypes.c_double()
+        _lib.check(self.lib.pdosgpu_time_kernel(self._w, int(which), int(reps), ctypes.byref(ms)),
+                   "pdosgpu_time_kernel", self.lib)
+        return ms.value
+
+    def close(self):
+        if self._w:
+            self.lib.pdosgpu_free(self._w)
+            self._w = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def solve_problem(prob, precision="fp64", scaling="2norm"):
+    """Set up, solve, fetch and free."""
+    with Workspace(prob, precision, scaling) as ws:
+        return ws.solve().fetch()
+
+
+def pdos_call(prob, precision=None, scaling=None, libname="libpdosindir.so"):
+    """Solve through the reference-compatible ``pdos()`` / ``pdos_ex()``."""
+    lib = _lib.load(libname)
+    mar = Marshalled(prob)
+    if precision is None and scaling is None:
+        solp = lib.pdos(ctypes.byref(mar.data), ctypes.byref(mar.cone))
+        info = None
+    else:
+        opt = make_options(precision or "fp64", scaling or "2norm")
+        info = _lib.Info()
+        solp = lib.pdos_ex(ctypes.byref(mar.data), ctypes.byref(mar.cone), ctypes.byref(opt),
+                           ctypes.byref(info))
+    if not solp:
+        raise RuntimeError(f"pdos returned NULL: {_lib.last_error(lib)}")
+    x, s, y, status = read_sol(solp, prob.n, prob.m)
+    lib.freeSol(ctypes.byref(solp))
+    out = {"x": x, "s": s, "y": y, "status": status}
+    if info is not None:
+        out["iters"] = info.admm_iters
+        out["cg_iters"] = info.cg_iters
+    return out
+
+
+# --------------------------------------------------------------------------
+# solve(c, A, b, dims, opts, x0, y0, s0): the reference's Python interface.
+
+def _is_int(v):
+    return isinstance(v, (int, np.integer)) and not isinstance(v, bool)
+
+
+def solve(c, A, b, dims, opts=None, x0=None, y0=None, s0=None, precision="fp64",
+          scaling="2norm"):
+    """Solve min c'x s.t. Ax + s = b, s in K (pdosmodule.c:27-344).
+
+    A is a scipy sparse matrix (converted to CSC), b and c dense vectors,
+    ``dims`` a dict with 'f', 'l' and 'q', ``opts`` an optional dict of
+    MAX_ITERS, EPS_ABS, ALPHA, VERBOSE, NORMALIZE, CG_MAX_ITS, CG_TOL.
+    Returns {'x', 's', 'y', 'status'}."""
+    import scipy.sparse as sp
+    if not sp.issparse(A):
+        raise TypeError("A must be a sparse 'd' matrix")
+    A = sp.csc_matrix(A, dtype=np.float64)
+    m, n = A.shape
+    if m <= 0:
+        raise ValueError("m must be a positive integer")
+    if n <= 0:
+        raise ValueError("n must be a positive integer")
+    c = np.asarray(c, dtype=np.float64).reshape(-1)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    if c.shape[0] != n:
+        raise ValueError("c has incompatible dimension with A")
+    if b.shape[0] != m:
+        raise ValueError("b has incompatible dimension with A")
+    if not isinstance(dims, dict):
+        raise TypeError("dims must be a dict")
+    f = dims.get("f", 0)
+    if not (_is_int(f) and f >= 0):
+        raise TypeError("dims['f'] ought to be a nonnegative integer")
+    l = dims.get("l", 0)
+    if not (_is_int(l) and l >= 0):
+        raise TypeError("dims['l'] ought to be a nonnegative integer")
+    q = dims.get("q", [])
+    if not isinstance(q, (list, tuple)):
+        raise TypeError("dims['q'] ought to be a list")
+    for qi in q:
+        if not (_is_int(qi) and qi > 0):
+            raise TypeError("dims['q'] ought to be a list of positive integers")
+    if f + l + sum(q) != m:
+        raise ValueError("Number of rows of G does not match dims.f+dims.l+sum(dims.q)")
+    p = dict(DEFAULT_PARAMS, VERBOSE=1)
+    if opts is not None:
+        if not isinstance(opts, dict):
+            raise TypeError("opts must be a dict")
+        if "MAX_ITERS" in opts:
+            v = opts["MAX_ITERS"]
+            if not (_is_int(v) and v >= 0):
+                raise TypeError("opts['MAX_ITERS'] ought to be a nonnegative integer")
+            p["MAX_ITERS"] = int(v)
+        for key in ("VERBOSE", "NORMALIZE"):
+            if key in opts:
+                if not isinstance(opts[key], bool):
+                    raise TypeError(f"opts['{key}'] ought to be a boolean")
+                p[key] = int(opts[key])
+        if "EPS_ABS" in opts:
+            v = opts["EPS_ABS"]
+            if not (isinstance(v, float) and v >= 0.0):
+                raise TypeError("opts['EPS_ABS'] ought to be a positive floating point value")
+            p["EPS_ABS"] = v
+        if "ALPHA" in opts:
+            v = opts["ALPHA"]
+            if not isinstance(v, float):
+                raise TypeError("opts['ALPHA'] ought to be a floating point value")
+            if v >= 2.0 or v <= 0.0:
+                raise TypeError("opts['ALPHA'] ought to be a floating point value between 0 and 2 "
+                                "(noninclusive)")
+            p["ALPHA"] = v
+        if "CG_MAX_ITS" in opts:
+            v = opts["CG_MAX_ITS"]
+            if not (_is_int(v) and v >= 0):
+                raise TypeError("opts['CG_MAX_ITS'] ought to be a nonnegative integer")
+            p["CG_MAX_ITS"] = int(v)
+        if "CG_TOL" in opts:
+            v = opts["CG_TOL"]
+            if not (isinstance(v, float) and v >= 0.0):
+                raise TypeError("opts['CG_TOL'] ought to be a positive floating point value")
+            p["CG_TOL"] = v
+
+    def vec(v, length, name):
+        if v is None:
+            return None
+        v = np.asarray(v, dtype=np.float64).reshape(-1)
+        if v.shape[0] != length:
+            raise ValueError(f"{name} has incompatible dimension with A")
+        return v
+
+    prob = Problem(n, m, A.data, A.indices.astype(np.int64), A.indptr.astype(np.int64), b, c,
+                   int(f), int(l), np.asarray(q, np.int64), p,
+                   vec(x0, n, "x0"), vec(y0, m, "y0"), vec(s0, m, "s0"))
+    res = solve_problem(prob, precision, scaling)
+    return {"x": res["x"], "s": res["s"], "y": res["y"], "status": res["status"]}
