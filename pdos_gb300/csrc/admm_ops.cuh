@@ -19,7 +19,7 @@
 #pragma once
 
 #include "common.cuh"
-#include "spmv.cuh"
+#include "sell.cuh"
 
 namespace pdosgpu {
 
@@ -59,7 +59,7 @@ struct OpPrep {
   T lam;
   DevState *S;
   __device__ bool begin(Ctx &) const { return true; }
-  __device__ void gather(const Ctx &, int i, T (&o)[1]) const { o[0] = V.x[i]; }
+  __device__ const T *src(const Ctx &, int) const { return V.x; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&red)[2]) const {
     const T ax = sum[0], sv = V.s[r], bv = V.b[r], yv = V.y[r];
     V.ax[r] = ax;
@@ -83,10 +83,7 @@ struct OpTop {
   T lam;
   DevState *S;
   __device__ bool begin(Ctx &) const { return !*(volatile int *)&S->done; }
-  __device__ void gather(const Ctx &, int i, T (&o)[2]) const {
-    o[0] = V.y[i];
-    o[1] = V.u[i];
-  }
+  __device__ const T *src(const Ctx &, int v) const { return v == 0 ? V.y : V.u; }
   __device__ void row(const Ctx &, int j, const T (&sum)[2], double (&red)[3]) const {
     const T cj = V.c[j];
     const T dr = (cj + sum[0]) / V.E[j];
@@ -109,61 +106,47 @@ struct OpTop {
         s.eta < s.eps * (1.0 + fabs(s.p_obj) + fabs(s.d_obj))) {
       s.solved = 1;
       s.done = 1;
+      s.cg_skip = 1;
       return;
     }
     s.qsold = tot[2];
     s.cg_iter = 0;
-    s.p_lazy = 0;
     s.cg_active = (s.cg_max > 0 && s.qsold > s.tol_sq) ? 1 : 0;
+    s.cg_skip = s.cg_active ? 0 : 1;
   }
 };
 
-struct CgCtx {
-  int lazy;
-  double ratio;
-};
-
-__device__ __forceinline__ bool cg_begin(const DevState *S, CgCtx &c) {
+__device__ __forceinline__ bool cg_begin(const DevState *S) {
   const volatile DevState *v = S;
-  if (v->done || !v->cg_active) return false;
-  c.lazy = v->p_lazy;
-  c.ratio = v->ratio;
-  return true;
+  return !v->done && v->cg_active;
 }
 
-// CG: u = A p, where p = ratio * p_prev + q is formed on the fly while the
-// previous iteration's direction update is pending (p_lazy).
+// CG: u = A p  (indirect/private.c:70)
 template <typename T>
 struct OpCgA {
   static constexpr int NV = 1, NR = 0;
-  using Ctx = CgCtx;
+  using Ctx = NoCtx;
   Vecs<T> V;
   DevState *S;
-  __device__ bool begin(Ctx &c) const { return cg_begin(S, c); }
-  __device__ void gather(const Ctx &c, int i, T (&o)[1]) const {
-    o[0] = c.lazy ? (T)c.ratio * V.p[i] + V.q[i] : V.p[i];
-  }
+  __device__ bool begin(Ctx &) const { return cg_begin(S); }
+  __device__ const T *src(const Ctx &, int) const { return V.p; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&)[1]) const {
     V.u[r] = sum[0];
   }
   __device__ void finalize(const Ctx &, const double (&)[1]) const {}
 };
 
-// CG: t = p + A'(Ap), p't; commits the pending direction update of p.
+// CG: t = p + A'(Ap) and p't  (indirect/private.c:71-75)
 template <typename T>
 struct OpCgAt {
   static constexpr int NV = 1, NR = 1;
-  using Ctx = CgCtx;
+  using Ctx = NoCtx;
   Vecs<T> V;
   DevState *S;
-  __device__ bool begin(Ctx &c) const { return cg_begin(S, c); }
-  __device__ void gather(const Ctx &, int i, T (&o)[1]) const { o[0] = V.u[i]; }
-  __device__ void row(const Ctx &c, int j, const T (&sum)[1], double (&red)[1]) const {
-    T pj = V.p[j];
-    if (c.lazy) {
-      pj = (T)c.ratio * pj + V.q[j];
-      V.p[j] = pj;
-    }
+  __device__ bool begin(Ctx &) const { return cg_begin(S); }
+  __device__ const T *src(const Ctx &, int) const { return V.u; }
+  __device__ void row(const Ctx &, int j, const T (&sum)[1], double (&red)[1]) const {
+    const T pj = V.p[j];
     const T tj = pj + sum[0];
     V.t[j] = tj;
     red[0] += (double)pj * (double)tj;
@@ -208,10 +191,27 @@ __global__ void __launch_bounds__(BLOCK) cg_update_kernel(Vecs<T> V, DevState *S
     } else {
       s.ratio = qsnew / s.qsold;
       s.qsold = qsnew;
-      s.p_lazy = 1;
       if (s.cg_iter >= s.cg_max) s.cg_active = 0;
     }
+    s.cg_skip = s.cg_active ? 0 : 1;
   }
+}
+
+// CG direction: p = beta p + q while CG continues (indirect/private.c:91-93)
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) cg_direction_kernel(Vecs<T> V, const DevState *S) {
+  __shared__ double s_ratio;
+  __shared__ int s_go;
+  if (threadIdx.x == 0) {
+    const volatile DevState *v = S;
+    s_go = (!v->done && v->cg_active) ? 1 : 0;
+    s_ratio = v->ratio;
+  }
+  __syncthreads();
+  if (!s_go) return;
+  const T beta = (T)s_ratio;
+  for (int j = blockIdx.x * BLOCK + threadIdx.x; j < V.n; j += gridDim.x * BLOCK)
+    V.p[j] = beta * V.p[j] + V.q[j];
 }
 
 // End of an ADMM iteration: bookkeeping done by the last block of the last
@@ -221,6 +221,7 @@ __device__ __forceinline__ void end_iteration(DevState *S, const double (&tot)[2
   S->by = tot[1];
   S->admm_iter += 1;
   if (S->admm_iter >= S->max_iters) S->done = 1;
+  S->cg_skip = 1;
 }
 
 // After CG: s~ = b - A x, relax, s = s~ - lam y; zero-cone and orthant rows
@@ -233,7 +234,7 @@ struct OpPost {
   T lam, alpha, one_minus_alpha;
   DevState *S;
   __device__ bool begin(Ctx &) const { return !*(volatile int *)&S->done; }
-  __device__ void gather(const Ctx &, int i, T (&o)[1]) const { o[0] = V.x[i]; }
+  __device__ const T *src(const Ctx &, int) const { return V.x; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&red)[2]) const {
     const T ax = sum[0];
     T stv = V.b[r] + (-ax);
@@ -444,7 +445,7 @@ struct OpAxpy {
   T sc;
   int accum;
   __device__ bool begin(Ctx &) const { return true; }
-  __device__ void gather(const Ctx &, int i, T (&o)[1]) const { o[0] = x[i]; }
+  __device__ const T *src(const Ctx &, int) const { return x; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&)[1]) const {
     const T v = sc * sum[0];
     y[r] = accum ? y[r] + v : v;

@@ -60,28 +60,15 @@ static int spmv_impl(int32_t rows, const int32_t *rowptr, const int32_t *colidx,
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
   for (int32_t r = 0; r < rows; ++r)
     if (rp[r + 1] < rp[r] || rp[0] != 0) return fail(PDOSGPU_EINVAL, "rowptr is not nondecreasing from 0");
-  SpmvPlan<T> plan;
-  build_tiles(rp.data(), rows, kTileNnz, kMaxTileRows, plan.tiles_h, plan.longs_h, plan.slots);
+  const int32_t nnz = rp[rows];
+  if (nnz > 0 && (!colidx || !val)) return fail(PDOSGPU_EINVAL, "NULL pointer");
+  // plan (slices of the caller's rows) and its scratch, freed on return
   DeviceArena arena;
-  PDOS_TRY(arena.alloc(&plan.tiles, plan.tiles_h.size()));
-  PDOS_TRY(arena.alloc(&plan.longs, plan.longs_h.size() + 1));
-  PDOS_TRY(arena.alloc(&plan.chunk_partial, (size_t)plan.slots + 1));
-  PDOS_TRY(arena.alloc(&plan.long_ticket, plan.longs_h.size() + 1));
-  PDOS_CUDA_TRY(cudaMemcpyAsync(plan.tiles, plan.tiles_h.data(), sizeof(Tile) * plan.tiles_h.size(),
-                                cudaMemcpyHostToDevice, st));
-  if (!plan.longs_h.empty())
-    PDOS_CUDA_TRY(cudaMemcpyAsync(plan.longs, plan.longs_h.data(), sizeof(LongRow) * plan.longs_h.size(),
-                                  cudaMemcpyHostToDevice, st));
-  PDOS_CUDA_TRY(cudaMemsetAsync(plan.long_ticket, 0, sizeof(unsigned) * (plan.longs_h.size() + 1), st));
-  int dev = 0, sms = 1, per_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spmv_kernel<T, kBlock, kTileNnz, OpAxpy<T>>,
-                                                kBlock, sizeof(T) * kTileNnz);
-  int grid = std::max(1, std::min<int>((int)plan.tiles_h.size(), std::max(per_sm, 1) * sms));
-  GridReduce none{nullptr, nullptr, 0, grid, 0};
-  spmv_kernel<T, kBlock, kTileNnz, OpAxpy<T>><<<grid, kBlock, sizeof(T) * kTileNnz, st>>>(
-      CsrDev<T>{rowptr, colidx, val, rows}, plan.view(), OpAxpy<T>{x, y, sc, accum}, none);
+  SellPlan<T> plan;
+  PDOS_TRY(plan.build(rp.data(), rows, colidx, val, arena, st));
+  plan.spmv(x, nullptr, nullptr, st);
+  GridReduce none{nullptr, nullptr, 0, plan.combine_grid, 0};
+  plan.combine(OpAxpy<T>{x, y, sc, accum}, none, st);
   PDOS_CUDA_TRY(cudaGetLastError());
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before the plan is freed
   return PDOSGPU_OK;

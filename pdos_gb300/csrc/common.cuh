@@ -121,7 +121,9 @@ struct DevState {
   // last residuals (reported)
   double p_res, d_res, p_obj, d_obj, eta;
   long long admm_iter, cg_total;
-  int cg_iter, cg_active, p_lazy, done, solved, evaluated;
+  int cg_iter, cg_active, done, solved, evaluated;
+  int cg_skip;  // done || !cg_active, read by the CG SpMV kernels
+  int error;  // set by a kernel whose bounded wait timed out
 };
 
 }  // namespace pdosgpu

@@ -12,9 +12,7 @@
 
 namespace pdosgpu {
 
-namespace {
-
-int g_num_sms = 0;
+static thread_local int g_num_sms = 0;
 
 int num_sms() {
   if (g_num_sms == 0) {
@@ -25,6 +23,8 @@ int num_sms() {
   }
   return g_num_sms;
 }
+
+namespace {
 
 inline int grid1d(int64_t n, int block = 256) {
   int64_t g = (n + block - 1) / block;
@@ -42,6 +42,8 @@ int persistent_grid(K kernel, int block, size_t smem, int work) {
   if (work < g) g = work;
   return g < 1 ? 1 : g;
 }
+
+
 
 double now_ms() {
   using namespace std::chrono;
@@ -160,7 +162,7 @@ class Engine : public EngineBase {
   // matrix in both layouts
   int32_t *Rp_ = nullptr, *Rj_ = nullptr, *Ap_ = nullptr, *Ai_ = nullptr;
   T *Rx_ = nullptr, *Ax_ = nullptr;
-  SpmvPlan<T> planA_, planT_;
+  SellPlan<T> sellA_, sellT_;  // A x (rows of A) and A' y (rows of A')
   // vectors
   Vecs<T> V_{};
   T *x_init_ = nullptr, *s_init_ = nullptr, *y_init_ = nullptr;
@@ -172,7 +174,8 @@ class Engine : public EngineBase {
   ConeTables ct_{};
   int soc_grid_ = 0, socbig_grid_ = 0;
   // grids
-  int grid_prep_ = 1, grid_top_ = 1, grid_cga_ = 1, grid_cgat_ = 1, grid_upd_ = 1, grid_post_ = 1;
+  int grid_upd_ = 1;
+  int grid_dir_ = 1;
 };
 
 template <typename T>
@@ -238,10 +241,14 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   PDOS_TRY(tmp.alloc(&b0, (size_t)m));
   PDOS_TRY(tmp.alloc(&c0, (size_t)n));
   PDOS_TRY(tmp.alloc(&err, 1));
-  PDOS_TRY(arena_.alloc(&Ap_, (size_t)n + 1));
+  // row pointer, index and value arrays are padded so that the SpMV's
+  // 16-byte aligned bulk-copy windows stay inside the allocations
+  PDOS_TRY(arena_.alloc(&Ap_, (size_t)n + 16));
   PDOS_TRY(arena_.alloc(&Ai_, (size_t)nnz + 16));
-  PDOS_TRY(arena_.alloc(&Rp_, (size_t)m + 1));
+  PDOS_TRY(arena_.alloc(&Rp_, (size_t)m + 16));
   PDOS_TRY(arena_.alloc(&Rj_, (size_t)nnz + 16));
+  PDOS_CUDA_TRY(cudaMemsetAsync(Ap_, 0, sizeof(int32_t) * ((size_t)n + 16), st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(Rp_, 0, sizeof(int32_t) * ((size_t)m + 16), st));
   PDOS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
   if (nnz > 0) {
     PDOS_CUDA_TRY(cudaMemcpyAsync(Ai64, pr.Ai, sizeof(int64_t) * nnz, cudaMemcpyHostToDevice, st));
@@ -274,14 +281,12 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
 
   // ---- equilibration in double
   double *Aw = nullptr, *bw = nullptr, *cw = nullptr, *xw = nullptr, *yw = nullptr, *sw = nullptr;
-  double *lam_d = nullptr;
   PDOS_TRY(tmp.alloc(&Aw, (size_t)nnz + 16));
   PDOS_TRY(tmp.alloc(&bw, (size_t)m));
   PDOS_TRY(tmp.alloc(&cw, (size_t)n));
   PDOS_TRY(tmp.alloc(&xw, (size_t)n));
   PDOS_TRY(tmp.alloc(&yw, (size_t)m));
   PDOS_TRY(tmp.alloc(&sw, (size_t)m));
-  PDOS_TRY(tmp.alloc(&lam_d, 1));
   PDOS_TRY(arena_.alloc(&D64_, (size_t)m));
   PDOS_TRY(arena_.alloc(&E64_, (size_t)n));
   PDOS_CUDA_TRY(cudaMemsetAsync(xw, 0, sizeof(double) * n, st));
@@ -414,12 +419,23 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
     PDOS_CUDA_TRY(cudaMemcpyAsync(cw, c0, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     PDOS_CUDA_TRY(cudaMemcpyAsync(bw, b0, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
   }
-  lambda_kernel<<<1, 32, 0, st>>>(bw, m, cw, n, ruiz ? 1e-6 : 1e-15, lam_d);
+  {
+    // lambda = (guard + ||b||) / (guard + ||c||) on the scaled data, summed
+    // sequentially on the host in the reference's order (common.h:182)
+    std::vector<double> hb(m), hc(n);
+    PDOS_CUDA_TRY(cudaMemcpyAsync(hb.data(), bw, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(hc.data(), cw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+    double sb = 0.0, sc = 0.0;
+    for (int i = 0; i < m; ++i) sb += hb[i] * hb[i];
+    for (int i = 0; i < n; ++i) sc += hc[i] * hc[i];
+    const double guard = ruiz ? 1e-6 : 1e-15;
+    lambda_ = (guard + std::sqrt(sb)) / (guard + std::sqrt(sc));
+  }
   scal_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1e3, 0);
   scal_kernel<<<grid1d(n), 256, 0, st>>>(cw, n, 1e3, 0);
   scal_kernel<<<grid1d(n), 256, 0, st>>>(xw, n, 1e3, 1);
   if (nnz > 0) scal_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, nnz, 1e3, 0);
-  PDOS_CUDA_TRY(cudaMemcpyAsync(&lambda_, lam_d, sizeof(double), cudaMemcpyDeviceToHost, st));
   PDOS_CUDA_TRY(cudaGetLastError());
 
   // ---- working arrays in T
@@ -468,59 +484,34 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   PDOS_TRY(arena_.alloc(&out_, (size_t)n + 2 * (size_t)m));
   PDOS_CUDA_TRY(cudaGetLastError());
 
-  // ---- tiles (host, from the two pointer arrays)
+  // ---- state (the plans record timeouts in it)
+  PDOS_TRY(arena_.alloc(&S_, 1));
+  PDOS_CUDA_TRY(cudaMallocHost(&host_state_, sizeof(DevState)));
+  PDOS_CUDA_TRY(cudaMemsetAsync(S_, 0, sizeof(DevState), st));
+
+  // ---- merge-path plans (host, from the two pointer arrays)
   {
     std::vector<int32_t> rp(m + 1), ap(n + 1);
     PDOS_CUDA_TRY(cudaMemcpyAsync(rp.data(), Rp_, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, st));
     PDOS_CUDA_TRY(cudaStreamSynchronize(st));
     for (int64_t j = 0; j <= n; ++j) ap[j] = (int32_t)pr.Ap[j];
-    SpmvPlan<T> *plans[2] = {&planA_, &planT_};
-    const std::vector<int32_t> *ptrs[2] = {&rp, &ap};
-    const int rows_of[2] = {m, n};
-    for (int k = 0; k < 2; ++k) {
-      SpmvPlan<T> &pl = *plans[k];
-      build_tiles(ptrs[k]->data(), rows_of[k], kTileNnz, kMaxTileRows, pl.tiles_h, pl.longs_h, pl.slots);
-      PDOS_TRY(arena_.alloc(&pl.tiles, pl.tiles_h.size()));
-      PDOS_TRY(arena_.alloc(&pl.longs, pl.longs_h.size()));
-      PDOS_TRY(arena_.alloc(&pl.chunk_partial, (size_t)pl.slots * 2 + 2));
-      PDOS_TRY(arena_.alloc(&pl.long_ticket, pl.longs_h.size() + 1));
-      if (!pl.tiles_h.empty())
-        PDOS_CUDA_TRY(cudaMemcpyAsync(pl.tiles, pl.tiles_h.data(), sizeof(Tile) * pl.tiles_h.size(),
-                                      cudaMemcpyHostToDevice, st));
-      if (!pl.longs_h.empty())
-        PDOS_CUDA_TRY(cudaMemcpyAsync(pl.longs, pl.longs_h.data(), sizeof(LongRow) * pl.longs_h.size(),
-                                      cudaMemcpyHostToDevice, st));
-      PDOS_CUDA_TRY(cudaMemsetAsync(pl.long_ticket, 0, sizeof(unsigned) * (pl.longs_h.size() + 1), st));
-    }
+    PDOS_TRY(sellA_.build(rp.data(), m, Rj_, Rx_, arena_, st));
+    PDOS_TRY(sellT_.build(ap.data(), n, Ai_, Ax_, arena_, st));
   }
   PDOS_TRY(build_cones(pr));
 
-  // ---- grids and reduction scratch
-  const int tA = (int)planA_.tiles_h.size(), tT = (int)planT_.tiles_h.size();
-  grid_prep_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpPrep<T>>, kBlock,
-                               sizeof(T) * kTileNnz, std::max(tA, 1));
-  grid_top_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpTop<T>>, kBlock,
-                              sizeof(T) * kTileNnz * 2, std::max(tT, 1));
-  grid_cga_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpCgA<T>>, kBlock,
-                              sizeof(T) * kTileNnz, std::max(tA, 1));
-  grid_cgat_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpCgAt<T>>, kBlock,
-                               sizeof(T) * kTileNnz, std::max(tT, 1));
-  grid_post_ = persistent_grid(spmv_kernel<T, kBlock, kTileNnz, OpPost<T>>, kBlock,
-                               sizeof(T) * kTileNnz, std::max(tA, 1));
+  // ---- grids and reduction scratch (an SpMV kernel uses grid+1 slots)
   grid_upd_ = persistent_grid(cg_update_kernel<T, kBlock>, kBlock, 0, (n + kBlock - 1) / kBlock);
+  grid_dir_ = std::max(1, std::min((n + kBlock - 1) / kBlock, num_sms() * 8));
   size_t slots = 0;
-  slots = std::max(slots, (size_t)grid_prep_ * 2);
-  slots = std::max(slots, (size_t)grid_top_ * 3);
-  slots = std::max(slots, (size_t)grid_cgat_);
+  slots = std::max(slots, (size_t)sellA_.combine_grid * 2);
+  slots = std::max(slots, (size_t)sellT_.combine_grid * 3);
   slots = std::max(slots, (size_t)grid_upd_);
-  slots = std::max(slots, (size_t)(grid_post_ + soc_grid_ + socbig_grid_) * 2);
+  slots = std::max(slots, (size_t)(sellA_.combine_grid + soc_grid_ + socbig_grid_) * 2);
   PDOS_TRY(arena_.alloc(&partials_, slots));
   PDOS_TRY(arena_.alloc(&tickets_, 8));
   PDOS_CUDA_TRY(cudaMemsetAsync(tickets_, 0, sizeof(unsigned) * 8, st));
 
-  // ---- state
-  PDOS_TRY(arena_.alloc(&S_, 1));
-  PDOS_CUDA_TRY(cudaMallocHost(&host_state_, sizeof(DevState)));
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
   tmp.release();
   PDOS_TRY(reset());
@@ -585,11 +576,10 @@ int Engine<T>::build_cones(const pdosgpu_problem &pr) {
 
 template <typename T>
 int Engine<T>::run_prep() {
-  GridReduce gr{partials_, tickets_ + 0, 0, grid_prep_, 1};
+  GridReduce gr{partials_, tickets_ + 0, 0, sellA_.combine_grid, 1};
   OpPrep<T> op{V_, (T)lambda_, S_};
-  spmv_kernel<T, kBlock, kTileNnz, OpPrep<T>>
-      <<<grid_prep_, kBlock, sizeof(T) * kTileNnz, stream_>>>(
-          CsrDev<T>{Rp_, Rj_, Rx_, m_}, planA_.view(), op, gr);
+  sellA_.spmv(V_.x, nullptr, nullptr, stream_);
+  sellA_.combine(op, gr, stream_);
   PDOS_CUDA_TRY(cudaGetLastError());
   launches += 1;
   return PDOSGPU_OK;
@@ -609,6 +599,7 @@ int Engine<T>::reset() {
   h.cg_max = cg_max_;
   h.p_res = h.d_res = h.p_obj = h.d_obj = h.eta = -1.0;
   h.done = max_iters_ <= 0 ? 1 : 0;
+  h.cg_skip = 1;
   *host_state_ = h;
   PDOS_CUDA_TRY(cudaMemcpyAsync(S_, host_state_, sizeof(DevState), cudaMemcpyHostToDevice, st));
   PDOS_CUDA_TRY(cudaMemcpyAsync(V_.x, x_init_, sizeof(T) * n_, cudaMemcpyDeviceToDevice, st));
@@ -627,35 +618,37 @@ int Engine<T>::reset() {
 template <typename T>
 int Engine<T>::build_graph() {
   cudaStream_t st = stream_;
-  const CsrDev<T> A{Rp_, Rj_, Rx_, m_};
-  const CsrDev<T> At{Ap_, Ai_, Ax_, n_};
   const T lam = (T)lambda_;
+  const int *done = &S_->done;
+  const int *cg_skip = &S_->cg_skip;
   auto top = [&]() {
-    GridReduce gr{partials_, tickets_ + 1, 0, grid_top_, 1};
-    spmv_kernel<T, kBlock, kTileNnz, OpTop<T>><<<grid_top_, kBlock, sizeof(T) * kTileNnz * 2, st>>>(
-        At, planT_.view(), OpTop<T>{V_, lam, S_}, gr);
+    GridReduce gr{partials_, tickets_ + 1, 0, sellT_.combine_grid, 1};
+    sellT_.spmv(V_.y, V_.u, done, st);
+    sellT_.combine(OpTop<T>{V_, lam, S_}, gr, st);
   };
   auto cg = [&]() {
-    GridReduce none{partials_, tickets_ + 2, 0, grid_cga_, 0};
-    spmv_kernel<T, kBlock, kTileNnz, OpCgA<T>><<<grid_cga_, kBlock, sizeof(T) * kTileNnz, st>>>(
-        A, planA_.view(), OpCgA<T>{V_, S_}, none);
-    GridReduce g2{partials_, tickets_ + 3, 0, grid_cgat_, 1};
-    spmv_kernel<T, kBlock, kTileNnz, OpCgAt<T>><<<grid_cgat_, kBlock, sizeof(T) * kTileNnz, st>>>(
-        At, planT_.view(), OpCgAt<T>{V_, S_}, g2);
+    GridReduce none{partials_, tickets_ + 2, 0, sellA_.combine_grid, 0};
+    sellA_.spmv(V_.p, nullptr, cg_skip, st);
+    sellA_.combine(OpCgA<T>{V_, S_}, none, st);
+    GridReduce g2{partials_, tickets_ + 3, 0, sellT_.combine_grid, 1};
+    sellT_.spmv(V_.u, nullptr, cg_skip, st);
+    sellT_.combine(OpCgAt<T>{V_, S_}, g2, st);
     GridReduce g3{partials_, tickets_ + 4, 0, grid_upd_, 1};
     cg_update_kernel<T, kBlock><<<grid_upd_, kBlock, 0, st>>>(V_, S_, g3);
+    cg_direction_kernel<T, kBlock><<<grid_dir_, kBlock, 0, st>>>(V_, S_);
   };
   auto tail = [&]() {
-    const int total = grid_post_ + soc_grid_ + socbig_grid_;
+    const int gpost = sellA_.combine_grid;
+    const int total = gpost + soc_grid_ + socbig_grid_;
     GridReduce g5{partials_, tickets_ + 5, 0, total, qsize_ == 0 ? 1 : 0};
     OpPost<T> op{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_};
-    spmv_kernel<T, kBlock, kTileNnz, OpPost<T>><<<grid_post_, kBlock, sizeof(T) * kTileNnz, st>>>(
-        A, planA_.view(), op, g5);
+    sellA_.spmv(V_.x, nullptr, done, st);
+    sellA_.combine(op, g5, st);
     if (qsize_ > 0) {
-      GridReduce g6{partials_, tickets_ + 6, grid_post_, total, socbig_grid_ == 0 ? 1 : 0};
+      GridReduce g6{partials_, tickets_ + 6, gpost, total, socbig_grid_ == 0 ? 1 : 0};
       soc_kernel<T, kBlock><<<soc_grid_, kBlock, 0, st>>>(V_, ct_, lam, S_, g6);
       if (socbig_grid_ > 0) {
-        GridReduce g7{partials_, tickets_ + 7, grid_post_ + soc_grid_, total, 1};
+        GridReduce g7{partials_, tickets_ + 7, gpost + soc_grid_, total, 1};
         soc_big_kernel<T, kBlock><<<socbig_grid_, kBlock, 0, st>>>(V_, ct_, lam, S_, g7);
       }
     }
@@ -776,6 +769,8 @@ int Engine<T>::iterate(int64_t iters, bool until_done) {
   }
   PDOS_TRY(read_state());
   solve_ms = now_ms() - t0;
+  if (host_state_->error)
+    return fail(PDOSGPU_ECUDA, "a device-side wait for a bulk copy timed out");
   return PDOSGPU_OK;
 }
 
@@ -824,49 +819,35 @@ template <typename T>
 int Engine<T>::time_kernel(int which, int reps, double *ms) {
   if (reps <= 0 || !ms) return fail(PDOSGPU_EINVAL, "reps must be positive");
   cudaStream_t st = stream_;
-  // make every kernel do its full work: not done, CG active, lazy update on
+  // make every kernel do its full work: not done, CG active
   PDOS_TRY(read_state());
   DevState h = *host_state_;
   h.done = 0;
   h.cg_active = 1;
-  h.p_lazy = 1;
+  h.cg_skip = 0;
   h.ratio = 0.5;
   h.qsold = 1.0;
   h.cg_iter = 0;
   h.max_iters = INT64_MAX / 2;
   *host_state_ = h;
   PDOS_CUDA_TRY(cudaMemcpyAsync(S_, host_state_, sizeof(DevState), cudaMemcpyHostToDevice, st));
-  const CsrDev<T> A{Rp_, Rj_, Rx_, m_};
-  const CsrDev<T> At{Ap_, Ai_, Ax_, n_};
-  const T lam = (T)lambda_;
   cudaEvent_t e0, e1;
   PDOS_CUDA_TRY(cudaEventCreate(&e0));
   PDOS_CUDA_TRY(cudaEventCreate(&e1));
   auto launch = [&]() {
     switch (which) {
-      case 0: {
-        GridReduce none{partials_, tickets_ + 2, 0, grid_cga_, 0};
-        spmv_kernel<T, kBlock, kTileNnz, OpCgA<T>><<<grid_cga_, kBlock, sizeof(T) * kTileNnz, st>>>(
-            A, planA_.view(), OpCgA<T>{V_, S_}, none);
+      case 0:  // CG A p
+        sellA_.spmv(V_.p, nullptr, nullptr, st);
         break;
-      }
-      case 1: {
-        GridReduce g2{partials_, tickets_ + 3, 0, grid_cgat_, 1};
-        spmv_kernel<T, kBlock, kTileNnz, OpCgAt<T>><<<grid_cgat_, kBlock, sizeof(T) * kTileNnz, st>>>(
-            At, planT_.view(), OpCgAt<T>{V_, S_}, g2);
+      case 1:  // CG A'(Ap)
+        sellT_.spmv(V_.u, nullptr, nullptr, st);
         break;
-      }
-      case 2: {
-        GridReduce gr{partials_, tickets_ + 1, 0, grid_top_, 0};
-        spmv_kernel<T, kBlock, kTileNnz, OpTop<T>><<<grid_top_, kBlock, sizeof(T) * kTileNnz * 2, st>>>(
-            At, planT_.view(), OpTop<T>{V_, lam, S_}, gr);
+      case 2:  // A'(y, u) of the iteration's first pass
+        sellT_.spmv(V_.y, V_.u, nullptr, st);
         break;
-      }
-      default: {
-        GridReduce g5{partials_, tickets_ + 5, 0, grid_post_, 0};
-        OpPost<T> op{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_};
-        spmv_kernel<T, kBlock, kTileNnz, OpPost<T>><<<grid_post_, kBlock, sizeof(T) * kTileNnz, st>>>(
-            A, planA_.view(), op, g5);
+      default: {  // epilogue of the CG A' pass
+        GridReduce g2{partials_, tickets_ + 3, 0, sellT_.combine_grid, 1};
+        sellT_.combine(OpCgAt<T>{V_, S_}, g2, st);
       }
     }
   };

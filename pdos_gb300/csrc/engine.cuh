@@ -2,17 +2,18 @@
 #pragma once
 
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "admm_ops.cuh"
 #include "common.cuh"
-#include "spmv.cuh"
+#include "sell.cuh"
 
 namespace pdosgpu {
 
 constexpr int kBlock = 256;
-constexpr int kTileNnz = 2048;
-constexpr int kMaxTileRows = 4 * kBlock;
+
+int num_sms();
 
 // Device allocations owned by one workspace, released together.
 class DeviceArena {
@@ -32,13 +33,6 @@ class DeviceArena {
     *p = static_cast<T *>(raw);
     return PDOSGPU_OK;
   }
-  void free_one(void *p) {
-    for (auto &q : ptrs_)
-      if (q == p) {
-        cudaFree(q);
-        q = nullptr;
-      }
-  }
   void release() {
     for (void *p : ptrs_)
       if (p) cudaFree(p);
@@ -49,17 +43,65 @@ class DeviceArena {
   std::vector<void *> ptrs_;
 };
 
+// Device side of a SELL plan (see sell.cuh), built from a host row pointer
+// array and the device index / value arrays of the same row-wise matrix.
 template <typename T>
-struct SpmvPlan {
-  std::vector<Tile> tiles_h;
-  std::vector<LongRow> longs_h;
-  int32_t slots = 0;
-  Tile *tiles = nullptr;
-  LongRow *longs = nullptr;
-  T *chunk_partial = nullptr;
-  unsigned int *long_ticket = nullptr;
-  TilesDev<T> view() const {
-    return TilesDev<T>{tiles, (int32_t)tiles_h.size(), longs, chunk_partial, long_ticket};
+struct SellPlan {
+  SellDev<T> dev{};
+  T *vsum = nullptr;  // [2 * nvr] virtual-row partials (scratch)
+  int spmv_grid = 1, combine_rows = 1, combine_grid = 1;
+
+  int build(const int32_t *ptr_h, int32_t rows, const int32_t *idx_d, const T *val_d,
+            DeviceArena &arena, cudaStream_t st) {
+    SellHost h;
+    h.build(ptr_h, rows);
+    int32_t *slice_off, *vr_len, *idx, *vr_ptr, *vr_list, *heavy, *slot_src;
+    T *val;
+    PDOS_TRY(arena.alloc(&slice_off, h.slice_off.size()));
+    PDOS_TRY(arena.alloc(&vr_len, h.vr_len.size()));
+    PDOS_TRY(arena.alloc(&vr_ptr, h.vr_ptr.size()));
+    PDOS_TRY(arena.alloc(&vr_list, h.vr_list.size()));
+    PDOS_TRY(arena.alloc(&heavy, h.heavy.size()));
+    PDOS_TRY(arena.alloc(&idx, (size_t)h.slots));
+    PDOS_TRY(arena.alloc(&val, (size_t)h.slots));
+    PDOS_TRY(arena.alloc(&vsum, (size_t)2 * h.nvr));
+    auto up = [&](int32_t *d, const std::vector<int32_t> &v) -> int {
+      if (!v.empty())
+        PDOS_CUDA_TRY(cudaMemcpyAsync(d, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, st));
+      return PDOSGPU_OK;
+    };
+    PDOS_TRY(up(slice_off, h.slice_off));
+    PDOS_TRY(up(vr_len, h.vr_len));
+    PDOS_TRY(up(vr_ptr, h.vr_ptr));
+    PDOS_TRY(up(vr_list, h.vr_list));
+    PDOS_TRY(up(heavy, h.heavy));
+    if (h.slots > 0) {
+      DeviceArena tmp;
+      PDOS_TRY(tmp.alloc(&slot_src, (size_t)h.slots));
+      PDOS_TRY(up(slot_src, h.slot_src));
+      const int g = (int)std::min<int64_t>((h.slots + 255) / 256, (int64_t)num_sms() * 16);
+      sell_fill_kernel<T><<<g, 256, 0, st>>>(slot_src, h.slots, idx_d, val_d, idx, val);
+      PDOS_CUDA_TRY(cudaGetLastError());
+      PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before slot_src is freed
+    }
+    dev = SellDev<T>{slice_off, vr_len, idx, val, h.nslices, h.nvr, vr_ptr, vr_list, heavy,
+                     (int32_t)h.heavy.size(), rows};
+    spmv_grid = std::max(1, std::min((h.nslices + 7) / 8, num_sms() * 8));
+    combine_rows = std::max(1, std::min((rows + 255) / 256, num_sms() * 8));
+    combine_grid = combine_rows + (int)h.heavy.size();
+    return PDOSGPU_OK;
+  }
+  // launch the SpMV into vsum; skip_a / skip_b: device flags (skip if
+  // *skip_a != 0 or *skip_b == 0), either may be NULL
+  void spmv(const T *x0, const T *x1, const int *skip, cudaStream_t st) const {
+    if (x1)
+      sell_spmv_kernel<T, 2, 256><<<spmv_grid, 256, 0, st>>>(dev, x0, x1, vsum, skip);
+    else
+      sell_spmv_kernel<T, 1, 256><<<spmv_grid, 256, 0, st>>>(dev, x0, x0, vsum, skip);
+  }
+  template <class Op>
+  void combine(const Op &op, GridReduce gr, cudaStream_t st) const {
+    sell_combine_kernel<T, 256, Op><<<combine_grid, 256, 0, st>>>(dev, vsum, op, gr, combine_rows);
   }
 };
 
