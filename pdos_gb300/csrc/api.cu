@@ -66,9 +66,8 @@ static int spmv_impl(int32_t rows, const int32_t *rowptr, const int32_t *colidx,
   DeviceArena arena;
   SellPlan<T> plan;
   PDOS_TRY(plan.build(rp.data(), rows, colidx, val, arena, st));
-  plan.spmv(x, nullptr, nullptr, st);
-  GridReduce none{nullptr, nullptr, 0, plan.combine_grid, 0};
-  plan.combine(OpAxpy<T>{x, y, sc, accum}, none, st);
+  GridReduce none{nullptr, nullptr, 0, plan.slots(), 0};
+  plan.run(x, nullptr, OpAxpy<T>{x, y, sc, accum}, none, st);
   PDOS_CUDA_TRY(cudaGetLastError());
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before the plan is freed
   return PDOSGPU_OK;

@@ -504,10 +504,10 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   grid_upd_ = persistent_grid(cg_update_kernel<T, kBlock>, kBlock, 0, (n + kBlock - 1) / kBlock);
   grid_dir_ = std::max(1, std::min((n + kBlock - 1) / kBlock, num_sms() * 8));
   size_t slots = 0;
-  slots = std::max(slots, (size_t)sellA_.combine_grid * 2);
-  slots = std::max(slots, (size_t)sellT_.combine_grid * 3);
+  slots = std::max(slots, (size_t)sellA_.slots() * 2);
+  slots = std::max(slots, (size_t)sellT_.slots() * 3);
   slots = std::max(slots, (size_t)grid_upd_);
-  slots = std::max(slots, (size_t)(sellA_.combine_grid + soc_grid_ + socbig_grid_) * 2);
+  slots = std::max(slots, (size_t)(sellA_.slots() + soc_grid_ + socbig_grid_) * 2);
   PDOS_TRY(arena_.alloc(&partials_, slots));
   PDOS_TRY(arena_.alloc(&tickets_, 8));
   PDOS_CUDA_TRY(cudaMemsetAsync(tickets_, 0, sizeof(unsigned) * 8, st));
@@ -576,10 +576,8 @@ int Engine<T>::build_cones(const pdosgpu_problem &pr) {
 
 template <typename T>
 int Engine<T>::run_prep() {
-  GridReduce gr{partials_, tickets_ + 0, 0, sellA_.combine_grid, 1};
-  OpPrep<T> op{V_, (T)lambda_, S_};
-  sellA_.spmv(V_.x, nullptr, nullptr, stream_);
-  sellA_.combine(op, gr, stream_);
+  GridReduce gr{partials_, tickets_ + 0, 0, sellA_.slots(), 1};
+  sellA_.run(V_.x, nullptr, OpPrep<T>{V_, (T)lambda_, S_}, gr, stream_);
   PDOS_CUDA_TRY(cudaGetLastError());
   launches += 1;
   return PDOSGPU_OK;
@@ -619,31 +617,25 @@ template <typename T>
 int Engine<T>::build_graph() {
   cudaStream_t st = stream_;
   const T lam = (T)lambda_;
-  const int *done = &S_->done;
-  const int *cg_skip = &S_->cg_skip;
   auto top = [&]() {
-    GridReduce gr{partials_, tickets_ + 1, 0, sellT_.combine_grid, 1};
-    sellT_.spmv(V_.y, V_.u, done, st);
-    sellT_.combine(OpTop<T>{V_, lam, S_}, gr, st);
+    GridReduce gr{partials_, tickets_ + 1, 0, sellT_.slots(), 1};
+    sellT_.run(V_.y, V_.u, OpTop<T>{V_, lam, S_}, gr, st);
   };
   auto cg = [&]() {
-    GridReduce none{partials_, tickets_ + 2, 0, sellA_.combine_grid, 0};
-    sellA_.spmv(V_.p, nullptr, cg_skip, st);
-    sellA_.combine(OpCgA<T>{V_, S_}, none, st);
-    GridReduce g2{partials_, tickets_ + 3, 0, sellT_.combine_grid, 1};
-    sellT_.spmv(V_.u, nullptr, cg_skip, st);
-    sellT_.combine(OpCgAt<T>{V_, S_}, g2, st);
+    GridReduce none{partials_, tickets_ + 2, 0, sellA_.slots(), 0};
+    sellA_.run(V_.p, nullptr, OpCgA<T>{V_, S_}, none, st);
+    GridReduce g2{partials_, tickets_ + 3, 0, sellT_.slots(), 1};
+    sellT_.run(V_.u, nullptr, OpCgAt<T>{V_, S_}, g2, st);
     GridReduce g3{partials_, tickets_ + 4, 0, grid_upd_, 1};
     cg_update_kernel<T, kBlock><<<grid_upd_, kBlock, 0, st>>>(V_, S_, g3);
     cg_direction_kernel<T, kBlock><<<grid_dir_, kBlock, 0, st>>>(V_, S_);
   };
   auto tail = [&]() {
-    const int gpost = sellA_.combine_grid;
+    const int gpost = sellA_.slots();
     const int total = gpost + soc_grid_ + socbig_grid_;
     GridReduce g5{partials_, tickets_ + 5, 0, total, qsize_ == 0 ? 1 : 0};
     OpPost<T> op{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_};
-    sellA_.spmv(V_.x, nullptr, done, st);
-    sellA_.combine(op, g5, st);
+    sellA_.run(V_.x, nullptr, op, g5, st);
     if (qsize_ > 0) {
       GridReduce g6{partials_, tickets_ + 6, gpost, total, socbig_grid_ == 0 ? 1 : 0};
       soc_kernel<T, kBlock><<<soc_grid_, kBlock, 0, st>>>(V_, ct_, lam, S_, g6);
@@ -831,23 +823,30 @@ int Engine<T>::time_kernel(int which, int reps, double *ms) {
   h.max_iters = INT64_MAX / 2;
   *host_state_ = h;
   PDOS_CUDA_TRY(cudaMemcpyAsync(S_, host_state_, sizeof(DevState), cudaMemcpyHostToDevice, st));
+  const T lam = (T)lambda_;
   cudaEvent_t e0, e1;
   PDOS_CUDA_TRY(cudaEventCreate(&e0));
   PDOS_CUDA_TRY(cudaEventCreate(&e1));
   auto launch = [&]() {
     switch (which) {
-      case 0:  // CG A p
-        sellA_.spmv(V_.p, nullptr, nullptr, st);
+      case 0: {  // CG u = A p
+        GridReduce none{partials_, tickets_ + 2, 0, sellA_.slots(), 0};
+        sellA_.run(V_.p, nullptr, OpCgA<T>{V_, S_}, none, st);
         break;
-      case 1:  // CG A'(Ap)
-        sellT_.spmv(V_.u, nullptr, nullptr, st);
+      }
+      case 1: {  // CG t = p + A'u, p't
+        GridReduce g2{partials_, tickets_ + 3, 0, sellT_.slots(), 1};
+        sellT_.run(V_.u, nullptr, OpCgAt<T>{V_, S_}, g2, st);
         break;
-      case 2:  // A'(y, u) of the iteration's first pass
-        sellT_.spmv(V_.y, V_.u, nullptr, st);
+      }
+      case 2: {  // A'(y, u) of the iteration's first pass
+        GridReduce gr{partials_, tickets_ + 1, 0, sellT_.slots(), 0};
+        sellT_.run(V_.y, V_.u, OpTop<T>{V_, lam, S_}, gr, st);
         break;
-      default: {  // epilogue of the CG A' pass
-        GridReduce g2{partials_, tickets_ + 3, 0, sellT_.combine_grid, 1};
-        sellT_.combine(OpCgAt<T>{V_, S_}, g2, st);
+      }
+      default: {  // A x of the iteration's last pass
+        GridReduce g5{partials_, tickets_ + 5, 0, sellA_.slots(), 0};
+        sellA_.run(V_.x, nullptr, OpPost<T>{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_}, g5, st);
       }
     }
   };

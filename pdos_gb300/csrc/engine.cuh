@@ -15,6 +15,10 @@ constexpr int kBlock = 256;
 
 int num_sms();
 
+#ifndef PDOS_SELL_BLOCKS_PER_SM
+#define PDOS_SELL_BLOCKS_PER_SM 16
+#endif
+
 // Device allocations owned by one workspace, released together.
 class DeviceArena {
  public:
@@ -55,13 +59,15 @@ struct SellPlan {
             DeviceArena &arena, cudaStream_t st) {
     SellHost h;
     h.build(ptr_h, rows);
-    int32_t *slice_off, *vr_len, *idx, *vr_ptr, *vr_list, *heavy, *slot_src;
+    int32_t *slice_off, *vr_len, *idx, *vr_ptr, *vr_list, *heavy, *slot_src, *vr_row, *split;
     T *val;
     PDOS_TRY(arena.alloc(&slice_off, h.slice_off.size()));
     PDOS_TRY(arena.alloc(&vr_len, h.vr_len.size()));
     PDOS_TRY(arena.alloc(&vr_ptr, h.vr_ptr.size()));
     PDOS_TRY(arena.alloc(&vr_list, h.vr_list.size()));
     PDOS_TRY(arena.alloc(&heavy, h.heavy.size()));
+    PDOS_TRY(arena.alloc(&vr_row, h.vr_row.size()));
+    PDOS_TRY(arena.alloc(&split, h.split.size()));
     PDOS_TRY(arena.alloc(&idx, (size_t)h.slots));
     PDOS_TRY(arena.alloc(&val, (size_t)h.slots));
     PDOS_TRY(arena.alloc(&vsum, (size_t)2 * h.nvr));
@@ -75,6 +81,8 @@ struct SellPlan {
     PDOS_TRY(up(vr_ptr, h.vr_ptr));
     PDOS_TRY(up(vr_list, h.vr_list));
     PDOS_TRY(up(heavy, h.heavy));
+    PDOS_TRY(up(vr_row, h.vr_row));
+    PDOS_TRY(up(split, h.split));
     if (h.slots > 0) {
       DeviceArena tmp;
       PDOS_TRY(tmp.alloc(&slot_src, (size_t)h.slots));
@@ -85,23 +93,32 @@ struct SellPlan {
       PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before slot_src is freed
     }
     dev = SellDev<T>{slice_off, vr_len, idx, val, h.nslices, h.nvr, vr_ptr, vr_list, heavy,
-                     (int32_t)h.heavy.size(), rows};
-    spmv_grid = std::max(1, std::min((h.nslices + 7) / 8, num_sms() * 8));
-    combine_rows = std::max(1, std::min((rows + 255) / 256, num_sms() * 8));
-    combine_grid = combine_rows + (int)h.heavy.size();
+                     (int32_t)h.heavy.size(), rows, vr_row, split, (int32_t)h.split.size(),
+                     h.ngiant};
+    vrow = h.vrow;
+    nvr = h.nvr;
+    spmv_grid = std::max(1, std::min((h.nslices + 7) / 8, num_sms() * PDOS_SELL_BLOCKS_PER_SM));
+    combine_rows = std::max(1, std::min(((int)h.split.size() + 255) / 256, num_sms() * 8));
+    combine_grid = combine_rows + h.ngiant + ((int)h.heavy.size() - h.ngiant + 7) / 8;
     return PDOSGPU_OK;
   }
-  // launch the SpMV into vsum; skip_a / skip_b: device flags (skip if
-  // *skip_a != 0 or *skip_b == 0), either may be NULL
-  void spmv(const T *x0, const T *x1, const int *skip, cudaStream_t st) const {
-    if (x1)
-      sell_spmv_kernel<T, 2, 256><<<spmv_grid, 256, 0, st>>>(dev, x0, x1, vsum, skip);
-    else
-      sell_spmv_kernel<T, 1, 256><<<spmv_grid, 256, 0, st>>>(dev, x0, x0, vsum, skip);
-  }
+  int vrow = 0, nvr = 0;
+  bool has_combine() const { return dev.nsplit + dev.nheavy > 0; }
+  // grid-reduction slots used by one run()
+  int slots() const { return spmv_grid + (has_combine() ? combine_grid : 0); }
+  // y-side of M x (x1 non-NULL: M x0 and M x1 at once), rows handed to `op`.
+  // `gr` describes this run's slot range; its final flag applies to the last
+  // kernel of the run.
   template <class Op>
-  void combine(const Op &op, GridReduce gr, cudaStream_t st) const {
-    sell_combine_kernel<T, 256, Op><<<combine_grid, 256, 0, st>>>(dev, vsum, op, gr, combine_rows);
+  void run(const T *x0, const T *x1, const Op &op, GridReduce gr, cudaStream_t st) const {
+    GridReduce g1 = gr;
+    if (has_combine()) g1.final_kernel = 0;
+    sell_spmv_kernel<T, 256, Op><<<spmv_grid, 256, 0, st>>>(dev, x0, x1 ? x1 : x0, vsum, op, g1);
+    if (has_combine()) {
+      GridReduce g2 = gr;
+      g2.base = gr.base + spmv_grid;
+      sell_combine_kernel<T, 256, Op><<<combine_grid, 256, 0, st>>>(dev, vsum, op, g2, combine_rows);
+    }
   }
 };
 

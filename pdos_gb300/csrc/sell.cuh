@@ -16,11 +16,14 @@
 // and no shared memory.  Lanes past their virtual row's length are predicated
 // off, so padding costs neither gathers nor FP64 work.
 //
-// The SpMV kernel writes one partial sum per virtual row.  The combine kernel
-// then walks the rows in natural order, adds each row's virtual-row partials
-// in order, and hands the sum to the epilogue functor `Op` (fused
-// element-wise work of the ADMM / CG step plus NR grid-wide sums).
-// Everything is deterministic for a fixed plan.
+// A row held by a single virtual row is finished in the SpMV kernel itself:
+// its sum goes straight to the epilogue functor `Op` (fused element-wise work
+// of the ADMM / CG step plus NR grid-wide sums).  A split row leaves one
+// partial per virtual row; the combine kernel adds a split row's partials in
+// order and runs its epilogue.  The virtual-row length is chosen per matrix:
+// whole rows when most nonzeros sit in short rows, short pieces when most
+// sit in long rows (so long rows spread over many lanes).  Everything is
+// deterministic for a fixed plan.
 #pragma once
 
 #include <algorithm>
@@ -31,9 +34,13 @@
 
 namespace pdosgpu {
 
-constexpr int kVrowMax = 256;   // nonzeros per virtual row (lane work unit)
+#ifndef PDOS_SELL_UNROLL
+#define PDOS_SELL_UNROLL 8
+#endif
+constexpr int kUnroll = PDOS_SELL_UNROLL; // loads in flight per lane
 constexpr int kSigma = 4096;    // sorting window, in virtual rows
-constexpr int kHeavyVrows = 64; // rows with more virtual rows: combined by a warp
+constexpr int kHeavyVrows = 64;    // rows with more pieces: combined by a warp
+constexpr int kGiantVrows = 2048;  // rows with more pieces: combined by a CTA
 
 // Host-side construction.  `ptr` is the row pointer array of a row-wise
 // matrix; the plan maps every slice slot to a source position (or -1).
@@ -47,10 +54,35 @@ struct SellHost {
   std::vector<int32_t> slot_src;   // [slots] source position or -1
   std::vector<int32_t> vr_ptr;     // [rows+1] virtual rows of each row ...
   std::vector<int32_t> vr_list;    // ... in chunk order (positions in slice order)
-  std::vector<int32_t> heavy;      // rows with more than kHeavyVrows virtual rows
+  std::vector<int32_t> heavy;      // rows with more than kHeavyVrows pieces,
+                                   // those above kGiantVrows first
+  int32_t ngiant = 0;
+  std::vector<int32_t> vr_row;     // [nvr] row of a whole-row virtual row, else -1
+  std::vector<int32_t> split;      // split rows with at most kHeavyVrows pieces
+  int32_t vrow = 0;                // nonzeros per virtual row
+
+  // Whole rows (up to 256) when at least half of the nonzeros sit in rows of
+  // at most 256; otherwise pieces of 32.
+  static int32_t choose_vrow(const int32_t *ptr, int32_t nrows) {
+    int64_t nnz = ptr[nrows], short_nz = 0;
+    int32_t longest_short = 1;
+    for (int32_t r = 0; r < nrows; ++r) {
+      const int32_t L = ptr[r + 1] - ptr[r];
+      if (L <= 256) {
+        short_nz += L;
+        longest_short = std::max(longest_short, L);
+      }
+    }
+    if (2 * short_nz < nnz) return 32;
+    int32_t v = 32;
+    while (v < longest_short) v *= 2;
+    return v;
+  }
 
   void build(const int32_t *ptr, int32_t nrows) {
     rows = nrows;
+    vrow = choose_vrow(ptr, nrows);
+    const int32_t kVrowMax = vrow;
     // virtual rows in natural order
     std::vector<int32_t> v_row, v_start, v_len;
     vr_ptr.assign(nrows + 1, 0);
@@ -63,8 +95,17 @@ struct SellHost {
         v_len.push_back(std::min(kVrowMax, L - c * kVrowMax) > 0 ? std::min(kVrowMax, L - c * kVrowMax) : 0);
       }
       vr_ptr[r + 1] = vr_ptr[r] + nch;
-      if (nch > kHeavyVrows) heavy.push_back(r);
+      if (nch > kHeavyVrows)
+        heavy.push_back(r);
+      else if (nch > 1)
+        split.push_back(r);
     }
+    std::stable_partition(heavy.begin(), heavy.end(), [&](int32_t r) {
+      return vr_ptr[r + 1] - vr_ptr[r] > kGiantVrows;
+    });
+    ngiant = 0;
+    for (int32_t r : heavy)
+      if (vr_ptr[r + 1] - vr_ptr[r] > kGiantVrows) ++ngiant;
     const int32_t nv = (int32_t)v_row.size();
     nvr = (nv + 31) / 32 * 32;
     // order: by length, longest first, stable, inside windows of kSigma
@@ -80,7 +121,12 @@ struct SellHost {
     vr_list.resize(nv);
     for (int32_t k = 0; k < nv; ++k) vr_list[k] = pos[k];  // natural virtual-row order -> position
     vr_len.assign(nvr, 0);
-    for (int32_t k = 0; k < nv; ++k) vr_len[k] = v_len[order[k]];
+    vr_row.assign(nvr, -1);
+    for (int32_t k = 0; k < nv; ++k) {
+      vr_len[k] = v_len[order[k]];
+      const int32_t r = v_row[order[k]];
+      if (vr_ptr[r + 1] - vr_ptr[r] == 1) vr_row[k] = r;
+    }
     nslices = nvr / 32;
     slice_off.assign(nslices + 1, 0);
     for (int32_t s = 0; s < nslices; ++s) {
@@ -113,6 +159,10 @@ struct SellDev {
   const int32_t *heavy;      // [nheavy]
   int32_t nheavy;
   int32_t rows;
+  const int32_t *vr_row;     // [nvr] row finished by this virtual row, or -1
+  const int32_t *split;      // [nsplit] split rows combined per thread
+  int32_t nsplit;
+  int32_t ngiant;            // heavy[0, ngiant): combined by a CTA each
 };
 
 // slot k of the plan takes the source entry slot_src[k] (or zero padding)
@@ -127,12 +177,20 @@ __global__ void sell_fill_kernel(const int32_t *slot_src, int64_t slots, const i
   }
 }
 
-// vsum[v * nvr + k] = sum over the k-th virtual row of val * x_v[idx]
-template <typename T, int NV, int BLOCK>
+// Each lane reduces one virtual row.  Whole rows go to the epilogue at once;
+// pieces of split rows are left in vsum[v * nvr + k] for the combine kernel.
+template <typename T, int BLOCK, class Op>
 __global__ void __launch_bounds__(BLOCK)
     sell_spmv_kernel(SellDev<T> S, const T *__restrict__ x0, const T *__restrict__ x1, T *vsum,
-                     const int *skip) {
-  if (skip && *(volatile const int *)skip) return;
+                     Op op, GridReduce gr) {
+  constexpr int NV = Op::NV;
+  constexpr int NR = Op::NR > 0 ? Op::NR : 1;
+  __shared__ double scratch[BLOCK / 32];
+  typename Op::Ctx ctx;
+  if (!op.begin(ctx)) return;
+  double red[NR];
+#pragma unroll
+  for (int k = 0; k < NR; ++k) red[k] = 0.0;
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (BLOCK / 32);
   for (int s = blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5); s < S.nslices; s += warps) {
@@ -141,16 +199,16 @@ __global__ void __launch_bounds__(BLOCK)
     const int len = __ldg(S.vr_len + vr);
     T acc0 = T(0), acc1 = T(0);
     int k = 0;
-    for (; k + 4 <= len; k += 4) {
-      int c[4];
-      T a[4];
+    for (; k + kUnroll <= len; k += kUnroll) {
+      int c[kUnroll];
+      T a[kUnroll];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < kUnroll; ++u) {
         c[u] = __ldg(S.idx + off + 32 * (k + u));
         a[u] = __ldg(S.val + off + 32 * (k + u));
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < kUnroll; ++u) {
         acc0 = fma(a[u], __ldg(x0 + c[u]), acc0);
         if (NV == 2) acc1 = fma(a[u], __ldg(x1 + c[u]), acc1);
       }
@@ -161,14 +219,26 @@ __global__ void __launch_bounds__(BLOCK)
       acc0 = fma(a, __ldg(x0 + c), acc0);
       if (NV == 2) acc1 = fma(a, __ldg(x1 + c), acc1);
     }
-    vsum[vr] = acc0;
-    if (NV == 2) vsum[S.nvr + vr] = acc1;
+    const int r = __ldg(S.vr_row + vr);
+    if (r >= 0) {
+      T sum[NV];
+      sum[0] = acc0;
+      if (NV == 2) sum[NV - 1] = acc1;
+      op.row(ctx, r, sum, red);
+    } else {
+      vsum[vr] = acc0;
+      if (NV == 2) vsum[S.nvr + vr] = acc1;
+    }
+  }
+  if constexpr (Op::NR > 0) {
+    double tot[NR];
+    if (grid_reduce<BLOCK, NR>(gr, red, tot, scratch) && threadIdx.x == 0) op.finalize(ctx, tot);
   }
 }
 
-// Rows in natural order: sum of the row's virtual rows (in chunk order),
-// then the epilogue.  Rows with many virtual rows are summed by a warp
-// (fixed tree) in the extra blocks after the per-thread ones.
+// Split rows: sum of the row's pieces (in chunk order), then the epilogue.
+// Rows with many pieces are summed by a warp each, rows with very many by a
+// CTA each (fixed trees), in the extra blocks after the per-thread ones.
 template <typename T, int BLOCK, class Op>
 __global__ void __launch_bounds__(BLOCK)
     sell_combine_kernel(SellDev<T> S, const T *__restrict__ vsum, Op op, GridReduce gr,
@@ -182,9 +252,9 @@ __global__ void __launch_bounds__(BLOCK)
 #pragma unroll
   for (int k = 0; k < NR; ++k) red[k] = 0.0;
   if ((int)blockIdx.x < row_blocks) {
-    for (int r = blockIdx.x * BLOCK + threadIdx.x; r < S.rows; r += row_blocks * BLOCK) {
+    for (int h = blockIdx.x * BLOCK + threadIdx.x; h < S.nsplit; h += row_blocks * BLOCK) {
+      const int r = __ldg(S.split + h);
       const int a = __ldg(S.vr_ptr + r), b = __ldg(S.vr_ptr + r + 1);
-      if (b - a > kHeavyVrows) continue;  // a heavy row: done by a warp below
       T sum[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) sum[v] = T(0);
@@ -195,16 +265,50 @@ __global__ void __launch_bounds__(BLOCK)
       }
       op.row(ctx, r, sum, red);
     }
-  } else {
-    // one heavy row per extra block, summed by its first warp
+  } else if ((int)blockIdx.x < row_blocks + S.ngiant) {
+    // a row with very many pieces per extra block: every thread sums a
+    // strided share of the pieces, then a fixed tree over the block
+    __shared__ T part[NV][BLOCK / 32];
     const int h = blockIdx.x - row_blocks;
-    if (h < S.nheavy && threadIdx.x < 32) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r = __ldg(S.heavy + h);
+    const int a = __ldg(S.vr_ptr + r), b = __ldg(S.vr_ptr + r + 1);
+    T sum[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sum[v] = T(0);
+    for (int q = a + threadIdx.x; q < b; q += BLOCK) {
+      const int p = __ldg(S.vr_list + q);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) sum[v] += vsum[(size_t)v * S.nvr + p];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
+    if (lane == 0)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) part[v][warp] = sum[v];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) sum[v] = lane < BLOCK / 32 ? part[v][lane] : T(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
+      if (lane == 0) op.row(ctx, r, sum, red);
+    }
+  } else {
+    // rows with many pieces: one per warp (strided partial sums, shuffle tree)
+    const int lane = threadIdx.x & 31;
+    const int h = S.ngiant + (blockIdx.x - row_blocks - S.ngiant) * (BLOCK / 32) + (threadIdx.x >> 5);
+    if (h < S.nheavy) {
       const int r = __ldg(S.heavy + h);
       const int a = __ldg(S.vr_ptr + r), b = __ldg(S.vr_ptr + r + 1);
       T sum[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) sum[v] = T(0);
-      for (int q = a + threadIdx.x; q < b; q += 32) {
+      for (int q = a + lane; q < b; q += 32) {
         const int p = __ldg(S.vr_list + q);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sum[v] += vsum[(size_t)v * S.nvr + p];
@@ -213,7 +317,7 @@ __global__ void __launch_bounds__(BLOCK)
       for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
         for (int v = 0; v < NV; ++v) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
-      if (threadIdx.x == 0) op.row(ctx, r, sum, red);
+      if (lane == 0) op.row(ctx, r, sum, red);
     }
   }
   if constexpr (Op::NR > 0) {
