@@ -13,8 +13,10 @@ JSON line (rank 0):
   e2e      solves/s through the drop-in pdos() with pinned host buffers: H2D
            of A, b, c, device set-up (transpose, equilibration), solve, D2H of
            x, s, y -- all inside the timed region
-  roofline the CG A' SpMV kernel (the dominant kernel), algorithmic bytes per
-           launch / mean launch time, against the measured HBM copy peak
+  roofline the SELL SpMV kernel of the CG A pass (u = A p, the kernel with the
+           largest share of the solve), algorithmic bytes per launch / mean
+           launch time (CUDA events on the solver's stream), against the
+           measured HBM copy peak; traffic from the committed ncu capture
   cpu_baseline  the oracle (C restatement of the reference, 1 core) on a
            bounded sample: set-up plus a few ADMM iterations, extrapolated
            to a full solve with the GPU's iteration count
@@ -122,6 +124,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def committed_traffic(workload, kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of this
+    workload (profiles/traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        d = json.load(fh)
+    return d.get(workload, {}).get(kernel)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -160,14 +173,15 @@ def dist_env():
 
 
 def spmv_bytes(prob, which, sv):
-    """Algorithmic bytes of one launch of the CG SpMV kernels (4-byte
-    indices): matrix values + indices + row pointers, each gathered vector
-    once, the epilogue's element-wise streams."""
+    """Algorithmic bytes of one launch of a CG SpMV kernel: matrix values and
+    4-byte indices, the gathered vector once, 8 bytes of per-row layout data
+    (length and row id), and the epilogue's element-wise streams.  Padding
+    and split-row partial sums are overhead, not counted."""
     nnz, m, N = prob.nnz, prob.m, prob.n
-    if which == 0:  # u = A p, p formed on the fly from p and q
-        return nnz * (sv + 4) + 4 * (m + 1) + 2 * N * sv + m * sv
-    # t = p + A'u, p committed: read u (gather), p, q; write p, t
-    return nnz * (sv + 4) + 4 * (N + 1) + m * sv + 4 * N * sv
+    if which == 0:  # u = A p: gather p (N), write u (m)
+        return nnz * (sv + 4) + N * sv + m * sv + 8 * m
+    # t = p + A'u: gather u (m), read p, write t (N)
+    return nnz * (sv + 4) + m * sv + 2 * N * sv + 8 * N
 
 
 def run_reference(args, wl, prob):
@@ -212,8 +226,9 @@ def config_of(args, wl, prob):
             "cones": {"f": prob.f, "l": prob.l, "q_count": int(len(prob.q)),
                       "q_max": int(max(prob.q)) if len(prob.q) else 0},
             "precision": wl["precision"], "params": wl["params"],
-            "l2": "inputs larger than L2 (A and A' resident, > 129 MB)" if prob.nnz * 8 > 2e8
-            else "small problem (L2-resident)",
+            "l2": ("inputs larger than L2: A and A' are %.0f MB resident in HBM, re-read by "
+                   "every SpMV (129 MB L2)" % (2 * prob.nnz * (12 if wl["precision"] == "fp64" else 8) / 1e6))
+            if 2 * prob.nnz * 8 > 129e6 else "small problem (L2-resident)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -227,11 +242,20 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="profiling case: set up the workload, run this many ADMM "
+                         "iterations, print nothing else (for ncu)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     prob = make_problem(wl)
     if args.impl == "reference":
         return run_reference(args, wl, prob)
+    if args.profile_iters:
+        from pdos_gb300.solver import Workspace
+        with Workspace(prob, wl["precision"]) as ws:
+            ws.iterate(args.profile_iters)
+            print("iterations", ws.fetch()["iters"])
+        return 0
 
     import torch
     ws_n, rank, local = dist_env()
@@ -281,21 +305,26 @@ def main():
     iters = int(np.median(iters_seen))
     cg_per_iter = res["cg_iters"] / max(res["iters"], 1)
 
-    # roofline of the dominant kernel (both CG SpMVs run k times per iteration)
-    ms_a = wsp.time_kernel(0, 20)
-    ms_t = wsp.time_kernel(1, 20)
+    # roofline of the dominant kernel: the SpMV of the CG A pass (launched
+    # k times per iteration, the largest share); the CG A' SpMV beside it
+    ms_a = wsp.time_kernel(4, 20)
+    ms_t = wsp.time_kernel(5, 20)
+    ms_pass_a = wsp.time_kernel(0, 20)
+    ms_pass_t = wsp.time_kernel(1, 20)
     wsp.reset()
-    which, ms_k = (1, ms_t) if ms_t >= ms_a else (0, ms_a)
     peak, peak_kind = measured_peaks()
-    alg = spmv_bytes(prob, which, sv)
-    achieved = alg / (ms_k / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "spmv_kernel<OpCgAt>" if which == 1 else "spmv_kernel<OpCgA>",
+    alg = spmv_bytes(prob, 0, sv)
+    achieved = alg / (ms_a / 1e3) / 1e9
+    traffic = committed_traffic(args.workload, "sell_spmv_kernel<OpCgA>")
+    roofline = {"bound": "hbm", "kernel": "sell_spmv_kernel<OpCgA> (u = A p)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_kind": peak_kind, "traffic": None, "bytes_per_launch": alg,
-                "ms_per_launch": ms_k,
-                "other_cg_kernel": {"ms_per_launch": ms_a if which == 1 else ms_t,
-                                    "achieved_GBs": spmv_bytes(prob, 1 - which, sv) /
-                                    ((ms_a if which == 1 else ms_t) / 1e3) / 1e9}}
+                "peak_kind": peak_kind, "traffic": traffic, "bytes_per_launch": alg,
+                "ms_per_launch": ms_a,
+                "cg_A_pass_ms_with_combine": ms_pass_a,
+                "other_cg_kernel": {"kernel": "sell_spmv_kernel<OpCgAt> (t = p + A'u)",
+                                    "ms_per_launch": ms_t,
+                                    "achieved_GBs": spmv_bytes(prob, 1, sv) / (ms_t / 1e3) / 1e9,
+                                    "pass_ms_with_combine": ms_pass_t}}
     # end to end through pdos() with pinned host buffers
     e2e = None
     if not args.no_e2e:

@@ -105,11 +105,12 @@ void pdosgpu_free(pdosgpu_work *w);
 void *pdosgpu_stream(pdosgpu_work *w);
 
 /* Kernel timing for roofline reports: launch one of the iteration's SpMV
- * kernels `reps` times back to back on the workspace stream between two
- * CUDA events and return the mean duration in ms.  which: 0 = CG A pass
- * (u = A p), 1 = CG A' pass (t = p + A'u), 2 = top A' pass on (y, u),
- * 3 = post A pass.  Leaves the iterate undefined: call pdosgpu_reset()
- * before solving again. */
+ * passes `reps` times back to back on the workspace stream between two CUDA
+ * events and return the mean duration in ms.  which: 0 = CG A pass
+ * (u = A p), 1 = CG A' pass (t = p + A'u), 2 = first A' pass on (y, u),
+ * 3 = last A pass on x (each with its split-row combine kernel, if any);
+ * 4 / 5 = the SpMV kernel alone of the CG A / A' pass.  Leaves the iterate
+ * undefined: call pdosgpu_reset() before solving again. */
 int pdosgpu_time_kernel(pdosgpu_work *w, int which, int reps, double *ms_per_launch);
 
 /* pdos() with explicit GPU options; info may be NULL. */

@@ -844,9 +844,21 @@ int Engine<T>::time_kernel(int which, int reps, double *ms) {
         sellT_.run(V_.y, V_.u, OpTop<T>{V_, lam, S_}, gr, st);
         break;
       }
-      default: {  // A x of the iteration's last pass
+      case 3: {  // A x of the iteration's last pass
         GridReduce g5{partials_, tickets_ + 5, 0, sellA_.slots(), 0};
         sellA_.run(V_.x, nullptr, OpPost<T>{V_, lam, (T)alpha_, (T)(1.0 - alpha_), S_}, g5, st);
+        break;
+      }
+      case 4: {  // the SpMV kernel of the CG A pass alone (no split-row combine)
+        GridReduce none{partials_, tickets_ + 2, 0, sellA_.slots(), 0};
+        sell_spmv_kernel<T, 256, OpCgA<T>><<<sellA_.spmv_grid, 256, 0, st>>>(
+            sellA_.dev, V_.p, V_.p, sellA_.vsum, OpCgA<T>{V_, S_}, none);
+        break;
+      }
+      default: {  // the SpMV kernel of the CG A' pass alone
+        GridReduce g2{partials_, tickets_ + 3, 0, sellT_.slots(), 0};
+        sell_spmv_kernel<T, 256, OpCgAt<T>><<<sellT_.spmv_grid, 256, 0, st>>>(
+            sellT_.dev, V_.u, V_.u, sellT_.vsum, OpCgAt<T>{V_, S_}, g2);
       }
     }
   };
