@@ -145,6 +145,23 @@ int pdosgpu_spmv_f32(int32_t rows, int32_t cols, const int32_t *rowptr,
 int pdosgpu_proj_cone_f64(double *v, int64_t f, int64_t l, int64_t qsize,
                           const int64_t *q, void *stream);
 
+/* The same projection as pdosgpu_proj_cone_f64, for callers that cannot
+ * allocate device memory while they run (memory owned by a pool allocator
+ * that must not be bypassed, regions where allocation is forbidden or would
+ * synchronise the device).  It calls no cudaMalloc/cudaFree: its scratch is a
+ * static device array of about 3 MB built into the library, held by every
+ * GPU that loads the library until the process exits.  Limits: at most 65,536
+ * second-order cones and 131,072 chunks of 4,096 rows (sum over cones of
+ * ceil(q[i]/4096)); larger requests return PDOSGPU_EINVAL without touching
+ * the GPU.  The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array, so calls whose work
+ * overlaps on the GPU race; serialise them on one stream.  q is a HOST
+ * array; the call returns once the work is queued on `stream`.  This entry
+ * point has no counterpart in the reference. */
+int pdosgpu_proj_cone_f64_noalloc(double *v, int64_t f, int64_t l, int64_t qsize,
+                                  const int64_t *q, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

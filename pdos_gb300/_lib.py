@@ -75,6 +75,8 @@ SIGNATURES = {
                                  c_float, c_void_p, c_int, c_void_p]),
     "pdosgpu_proj_cone_f64": (c_int, [c_void_p, c_int64, c_int64, c_int64, POINTER(c_int64),
                                       c_void_p]),
+    "pdosgpu_proj_cone_f64_noalloc": (c_int, [c_void_p, c_int64, c_int64, c_int64,
+                                              POINTER(c_int64), c_void_p]),
 }
 
 _libs = {}

@@ -32,12 +32,13 @@ UNITS = [
     ("api.o", "api.cu", ["-DPDOS_DLONG"]),
     ("batch.o", "batch.cu", ["-DPDOS_DLONG"]),
     ("mlp.o", "mlp.cu", ["-DPDOS_DLONG"]),
+    ("noalloc.o", "noalloc.cu", ["-DPDOS_DLONG"]),
     ("abi_l.o", "abi.cu", ["-DPDOS_DLONG"]),
     ("abi_i.o", "abi.cu", []),
 ]
 TARGETS = {
-    "libpdosindir.so": ["engine.o", "api.o", "batch.o", "mlp.o", "abi_l.o"],
-    "libpdosindir_i32.so": ["engine.o", "api.o", "batch.o", "mlp.o", "abi_i.o"],
+    "libpdosindir.so": ["engine.o", "api.o", "batch.o", "mlp.o", "noalloc.o", "abi_l.o"],
+    "libpdosindir_i32.so": ["engine.o", "api.o", "batch.o", "mlp.o", "noalloc.o", "abi_i.o"],
 }
 
 
