@@ -117,6 +117,60 @@ int pdosgpu_time_kernel(pdosgpu_work *w, int which, int reps, double *ms_per_lau
 Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt,
              pdosgpu_info *info);
 
+/* ---- batches of independent problems ----------------------------------
+ * Many problems of uneven sizes and cone profiles solved together: each
+ * instance runs the reference's indirect ADMM (pdos.c:50-132 with
+ * indirect/private.c:31-118) with its own parameters, lambda, scaling, CG
+ * and stop test; one CTA solves one instance at a time and takes the next
+ * one when it finishes.  Instances share NORMALIZE; Ruiz scaling is not
+ * available for batches.  An instance must fit one CTA's shared memory:
+ * max(m, n) + m + n (+ pieces of long rows) values of at most 225 KB. */
+typedef struct pdosgpu_batch pdosgpu_batch;
+
+/* Set up `count` problems (the work of pdosgpu_setup for each).
+ * iters_per_launch: ADMM iterations each instance runs per kernel launch
+ * (<= 0: 64); it bounds a launch's duration, not the solve. */
+int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count,
+                        const pdosgpu_options *opt, int iters_per_launch,
+                        pdosgpu_batch **out);
+/* Launch until every instance has passed its stop test or run MAX_ITERS. */
+int pdosgpu_batch_solve(pdosgpu_batch *b);
+/* At most `launches` more launches (stops early when all are done). */
+int pdosgpu_batch_launch(pdosgpu_batch *b, int64_t launches);
+/* Restore every instance's starting iterate. */
+int pdosgpu_batch_reset(pdosgpu_batch *b);
+/* New starting iterates from DEVICE arrays in the caller's (unscaled)
+ * units, stacked instance after instance (x: sum n, y and s: sum m); any
+ * may be NULL to keep the current one.  Scales them as pdosgpu_setup scales
+ * Data.x/y/s (common.h:147-161, :185-192) and resets the batch. */
+int pdosgpu_batch_warm_start(pdosgpu_batch *b, const double *x0, const double *y0,
+                             const double *s0);
+/* Unscaled solutions (pdos.c:251-294) of instances [first, first+count)
+ * into host arrays stacked the same way (any may be NULL), and one info
+ * record per instance (may be NULL). */
+int pdosgpu_batch_fetch(pdosgpu_batch *b, int64_t first, int64_t count, double *x,
+                        double *s, double *y, pdosgpu_info *info);
+/* Instances finished so far (negative on error). */
+int64_t pdosgpu_batch_done(pdosgpu_batch *b);
+/* Autotuner: times `iters` iterations of each size class at each CTA size
+ * (128, 256, 512), keeps the fastest, resets the batch; blocks (may be
+ * NULL) receives the choice for the four classes. */
+int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks);
+/* Set the CTA size of the four size classes explicitly. */
+int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks);
+/* Number of instances and stacked sizes (any may be NULL). */
+int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m,
+                        int64_t *nnz);
+void *pdosgpu_batch_stream(pdosgpu_batch *b);
+void pdosgpu_batch_free(pdosgpu_batch *b);
+
+/* pdos() over `count` problems at once: sols[i] is what pdos(d[i], k[i])
+ * returns (free each with freeSol), info (may be NULL) gets one record per
+ * instance.  Returns PDOSGPU_OK or a negative status (then every sols[i]
+ * is NULL). */
+int pdos_batch(const Data *const *d, const Cone *const *k, int64_t count,
+               const pdosgpu_options *opt, Sol **sols, pdosgpu_info *info);
+
 /* ---- kernel-level entry points on device memory ------------------------
  * Pointers are device pointers; `stream` is a cudaStream_t (NULL = legacy
  * default stream).  They run asynchronously on `stream`. */

@@ -77,6 +77,22 @@ SIGNATURES = {
                                       c_void_p]),
     "pdosgpu_proj_cone_f64_noalloc": (c_int, [c_void_p, c_int64, c_int64, c_int64,
                                               POINTER(c_int64), c_void_p]),
+    "pdosgpu_batch_setup": (c_int, [POINTER(Problem), c_int64, POINTER(Options), c_int,
+                                    POINTER(c_void_p)]),
+    "pdosgpu_batch_solve": (c_int, [c_void_p]),
+    "pdosgpu_batch_launch": (c_int, [c_void_p, c_int64]),
+    "pdosgpu_batch_reset": (c_int, [c_void_p]),
+    "pdosgpu_batch_warm_start": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pdosgpu_batch_fetch": (c_int, [c_void_p, c_int64, c_int64, _D, _D, _D, POINTER(Info)]),
+    "pdosgpu_batch_done": (c_int64, [c_void_p]),
+    "pdosgpu_batch_tune": (c_int, [c_void_p, c_int, POINTER(c_int)]),
+    "pdosgpu_batch_set_blocks": (c_int, [c_void_p, POINTER(c_int)]),
+    "pdosgpu_batch_sizes": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64),
+                                    POINTER(c_int64), POINTER(c_int64)]),
+    "pdosgpu_batch_stream": (c_void_p, [c_void_p]),
+    "pdosgpu_batch_free": (None, [c_void_p]),
+    "pdos_batch": (c_int, [POINTER(POINTER(Data)), POINTER(POINTER(Cone)), c_int64,
+                           POINTER(Options), POINTER(POINTER(Sol)), POINTER(Info)]),
 }
 
 _libs = {}

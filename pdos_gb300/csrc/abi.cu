@@ -31,16 +31,14 @@ void widen(const Data *d, const Cone *k, Wide &w) {
   w.qq = w.q.empty() ? nullptr : w.q.data();
 }
 
-}  // namespace
 
-extern "C" {
-
-Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt, pdosgpu_info *info) {
-  if (d == NULL || k == NULL) return NULL;  // pdos.c:61-63
-  if (d->p == NULL || d->Ap == NULL || d->n <= 0 || d->m <= 0) return NULL;
-  Wide w;
+// Data / Cone / Params of the reference (pdos.h:15-35, cones.h:8-13) as one
+// pdosgpu_problem; false for the inputs the reference rejects (pdos.c:61-63)
+// or cannot index.
+bool to_problem(const Data *d, const Cone *k, Wide &w, pdosgpu_problem &pr) {
+  if (d == NULL || k == NULL) return false;
+  if (d->p == NULL || d->Ap == NULL || d->n <= 0 || d->m <= 0) return false;
   widen(d, k, w);
-  pdosgpu_problem pr;
   std::memset(&pr, 0, sizeof(pr));
   pr.n = d->n;
   pr.m = d->m;
@@ -63,32 +61,96 @@ Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt, pdosgpu_i
   pr.cg_tol = d->p->CG_TOL;
   pr.verbose = d->p->VERBOSE;
   pr.normalize = d->p->NORMALIZE;
+  return true;
+}
 
+// A Sol allocated as pdos() allocates it (pdos.c:121, PDOS_malloc = malloc).
+Sol *new_sol(idxint n, idxint m) {
+  Sol *sol = (Sol *)malloc(sizeof(Sol));
+  if (!sol) return NULL;
+  std::memset(sol, 0, sizeof(Sol));
+  sol->n = n;
+  sol->m = m;
+  sol->x = (double *)malloc(sizeof(double) * n);
+  sol->s = (double *)malloc(sizeof(double) * m);
+  sol->y = (double *)malloc(sizeof(double) * m);
+  if (!sol->x || !sol->s || !sol->y) freeSol(&sol);
+  return sol;
+}
+
+// exactly the reference's two status strings (pdos.c:255-258)
+void set_status(Sol *sol, int solved) {
+  std::strncpy(sol->status, solved ? "Solved" : "Indeterminate", sizeof(sol->status) - 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt, pdosgpu_info *info) {
+  Wide w;
+  pdosgpu_problem pr;
+  if (!to_problem(d, k, w, pr)) return NULL;
   pdosgpu_work *work = NULL;
   if (pdosgpu_setup(&pr, opt, &work) != PDOSGPU_OK) return NULL;
   Sol *sol = NULL;
   if (pdosgpu_solve(work) == PDOSGPU_OK) {
-    sol = (Sol *)malloc(sizeof(Sol));
-    if (sol) {
-      std::memset(sol, 0, sizeof(Sol));
-      sol->n = d->n;
-      sol->m = d->m;
-      sol->x = (double *)malloc(sizeof(double) * d->n);
-      sol->s = (double *)malloc(sizeof(double) * d->m);
-      sol->y = (double *)malloc(sizeof(double) * d->m);
-      pdosgpu_info inf;
-      if (!sol->x || !sol->s || !sol->y ||
-          pdosgpu_fetch(work, sol->x, sol->s, sol->y, &inf) != PDOSGPU_OK) {
-        freeSol(&sol);
-      } else {
-        // exactly the reference's two status strings (pdos.c:255-258)
-        std::strncpy(sol->status, inf.solved ? "Solved" : "Indeterminate", sizeof(sol->status) - 1);
-        if (info) *info = inf;
-      }
+    sol = new_sol(d->n, d->m);
+    pdosgpu_info inf;
+    if (sol && pdosgpu_fetch(work, sol->x, sol->s, sol->y, &inf) != PDOSGPU_OK) {
+      freeSol(&sol);
+    } else if (sol) {
+      set_status(sol, inf.solved);
+      if (info) *info = inf;
     }
   }
   pdosgpu_free(work);
   return sol;
+}
+
+int pdos_batch(const Data *const *d, const Cone *const *k, int64_t count,
+               const pdosgpu_options *opt, Sol **sols, pdosgpu_info *info) {
+  if (!d || !k || !sols || count <= 0) return PDOSGPU_EINVAL;
+  for (int64_t i = 0; i < count; ++i) sols[i] = NULL;
+  std::vector<Wide> w(count);
+  std::vector<pdosgpu_problem> pr(count);
+  for (int64_t i = 0; i < count; ++i)
+    if (!to_problem(d[i], k[i], w[i], pr[i])) return PDOSGPU_EINVAL;
+  pdosgpu_batch *b = NULL;
+  int rc = pdosgpu_batch_setup(pr.data(), count, opt, 0, &b);
+  if (rc != PDOSGPU_OK) return rc;
+  rc = pdosgpu_batch_solve(b);
+  int64_t N = 0, M = 0;
+  if (rc == PDOSGPU_OK) rc = pdosgpu_batch_sizes(b, NULL, &N, &M, NULL);
+  std::vector<double> x, s, y;
+  std::vector<pdosgpu_info> inf;
+  if (rc == PDOSGPU_OK) {
+    x.resize(N);
+    s.resize(M);
+    y.resize(M);
+    inf.resize(count);
+    rc = pdosgpu_batch_fetch(b, 0, count, x.data(), s.data(), y.data(), inf.data());
+  }
+  pdosgpu_batch_free(b);
+  int64_t c0 = 0, r0 = 0;
+  for (int64_t i = 0; i < count && rc == PDOSGPU_OK; ++i) {
+    const int64_t n = d[i]->n, m = d[i]->m;
+    sols[i] = new_sol(d[i]->n, d[i]->m);
+    if (!sols[i]) {
+      rc = PDOSGPU_ENOMEM;
+      break;
+    }
+    std::memcpy(sols[i]->x, &x[c0], sizeof(double) * n);
+    std::memcpy(sols[i]->s, &s[r0], sizeof(double) * m);
+    std::memcpy(sols[i]->y, &y[r0], sizeof(double) * m);
+    set_status(sols[i], inf[i].solved);
+    if (info) info[i] = inf[i];
+    c0 += n;
+    r0 += m;
+  }
+  if (rc != PDOSGPU_OK)
+    for (int64_t i = 0; i < count; ++i) freeSol(&sols[i]);
+  return rc;
 }
 
 Sol *pdos(const Data *d, const Cone *k) { return pdos_ex(d, k, NULL, NULL); }

@@ -1,0 +1,1281 @@
+// Batched solver: many independent PDOS problems of uneven sizes and cone
+// profiles, solved by one persistent kernel per size class.
+//
+// Each CTA takes an instance from a queue and runs that instance's whole
+// ADMM iteration (pdos.c:94-120) with CTA barriers only: the A' pass on
+// (y, u) with the stop test, the warm-started CG (indirect/private.c:31-104),
+// the A pass on x with relaxation, zero / orthant projection and dual update
+// (pdos.c:232-249, :296-303), the second-order-cone projection
+// (cones.c:21-47).  The vector a product gathers from is staged in shared
+// memory, so the matrix streams from HBM with coalesced loads while the
+// random gathers hit shared memory; CG's p, A p and t never leave shared
+// memory.  A finished instance frees its CTA for the next one (convergence
+// masking), every reduction has a fixed order, and the kernel of one launch
+// runs each instance for at most `iter_cap` iterations, so a captured launch
+// can be replayed until every instance is done.
+//
+// Per-instance arithmetic follows the grid engine (admm_ops.cuh) operation
+// by operation; only the summation order of the products and reductions
+// differs.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "problem.cuh"
+
+namespace pdosgpu {
+namespace batch {
+
+constexpr int kLongRow = 128;  // rows with more nonzeros go to warp-wide pieces
+constexpr int kPiece = 256;    // target nonzeros per piece
+constexpr int kClasses = 4;    // size classes (by nonzeros per instance)
+constexpr int64_t kClassNnz[kClasses - 1] = {4096, 32768, 262144};
+constexpr int kSmemLimit = 225 * 1024;  // dynamic shared memory per CTA (opt-in limit 227 KB)
+constexpr int kBlocks[] = {128, 256, 512};
+constexpr int kNumBlocks = 3;
+
+// One side (A: rows of A; At: rows of A', i.e. columns of A) of an instance
+// in the hybrid layout: slices of 32 consecutive rows stored column-major
+// (lane = row), and rows longer than kLongRow cut into pieces of at most
+// kPiece nonzeros, one warp per piece.
+struct Side {
+  int64_t slice0, piece0, split0;
+  int32_t nslices, npieces, nsplit, rows;
+};
+
+struct Inst {
+  int64_t row0, col0;  // offsets into the stacked row / column vectors
+  int32_t m, n, f, l;
+  int64_t cone0;
+  int32_t ncones, cls;
+  Side A, At;
+  double lambda, pscale, dscale, alpha, eps, tol_sq;
+  int64_t max_iters, cg_max;
+};
+
+struct State {
+  double pres_sq, by, p_res, d_res, p_obj, d_obj, eta;
+  long long admm_iter, cg_total;
+  int solved, done, prepped, pad;
+};
+
+template <typename T>
+struct Hyb {
+  const int64_t *slice_beg;    // first element of each slice
+  const int32_t *slice_w;      // its width (elements per lane)
+  const uint32_t *slice_skip;  // lanes whose row is a long row or past the end
+  const int32_t *piece_row;    // >= 0: the whole row; < 0: ~row of a split row
+  const int64_t *piece_beg;
+  const int32_t *piece_len;
+  const int32_t *split_row, *split_p0, *split_np;  // pieces of each split row
+  const int32_t *idx;          // gather index, local to the instance
+  const T *val;
+};
+
+template <typename T>
+struct Dev {
+  const Inst *inst;
+  State *state;
+  const int32_t *order;        // instance ids, class by class
+  const int32_t *class_begin;  // [kClasses + 1]
+  int32_t *queue;              // [kClasses] queue heads, zeroed before a launch
+  int32_t *ndone;              // instances finished so far
+  T *x, *s, *y, *st, *u, *ax, *q;
+  const T *b, *c, *D, *E;
+  Hyb<T> A, At;
+  const int32_t *cone_off, *cone_len;  // local first row and size of each cone
+};
+
+// Shared-memory regions of one class, in elements of T.
+struct Smem {
+  int32_t g1, g2, tt, pb;
+  size_t bytes(size_t elem) const { return elem * ((size_t)g1 + g2 + tt + pb); }
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sums of N values; every thread adds the warp partials in the same
+// fixed order, so all threads get identical totals.  scratch: N * BLOCK/32.
+template <int BLOCK, int N>
+__device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
+  constexpr int W = BLOCK / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) v[k] = warp_sum(v[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) scratch[k * W + warp] = v[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    double t = 0.0;
+#pragma unroll 8
+    for (int w = 0; w < W; ++w) t += scratch[k * W + w];
+    v[k] = t;
+  }
+  __syncthreads();
+}
+
+// y-side of one product over one side of an instance: NV source vectors
+// (in shared or global memory), rows handed to epi(row, sum0, sum1).  Split
+// rows leave piece partials in pbuf and are finished after a barrier.
+template <typename T, int BLOCK, int NV, class Epi>
+__device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, const T *src0,
+                                            const T *src1, T *pbuf, Epi &&epi) {
+  constexpr int W = BLOCK / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = warp; k < sd.npieces; k += W) {
+    const int64_t pk = sd.piece0 + k;
+    const int32_t prow = H.piece_row[pk];
+    const int64_t beg = H.piece_beg[pk];
+    const int len = H.piece_len[pk];
+    T a0 = T(0), a1 = T(0);
+#pragma unroll 4
+    for (int e = lane; e < len; e += 32) {
+      const int j = H.idx[beg + e];
+      const T v = H.val[beg + e];
+      a0 = fma(v, src0[j], a0);
+      if (NV == 2) a1 = fma(v, src1[j], a1);
+    }
+    a0 = warp_sum_t(a0);
+    if (NV == 2) a1 = warp_sum_t(a1);
+    if (lane == 0) {
+      if (prow >= 0) {
+        epi(prow, a0, a1);
+      } else {
+        pbuf[k * NV] = a0;
+        if (NV == 2) pbuf[k * NV + 1] = a1;
+      }
+    }
+  }
+  for (int s = warp; s < sd.nslices; s += W) {
+    const int64_t sk = sd.slice0 + s;
+    const int64_t off = H.slice_beg[sk];
+    const int width = H.slice_w[sk];
+    T a0 = T(0), a1 = T(0);
+    const int32_t *ip = H.idx + off + lane;
+    const T *vp = H.val + off + lane;
+#pragma unroll 4
+    for (int c = 0; c < width; ++c) {
+      const int j = ip[c * 32];
+      const T v = vp[c * 32];
+      a0 = fma(v, src0[j], a0);
+      if (NV == 2) a1 = fma(v, src1[j], a1);
+    }
+    if (!((H.slice_skip[sk] >> lane) & 1u)) epi(s * 32 + lane, a0, a1);
+  }
+  if (sd.nsplit > 0) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < sd.nsplit; k += BLOCK) {
+      const int64_t sk = sd.split0 + k;
+      const int p0 = H.split_p0[sk], np = H.split_np[sk];
+      T a0 = T(0), a1 = T(0);
+      for (int t = 0; t < np; ++t) {
+        a0 += pbuf[(p0 + t) * NV];
+        if (NV == 2) a1 += pbuf[(p0 + t) * NV + 1];
+      }
+      epi(H.split_row[sk], a0, a1);
+    }
+  }
+}
+
+// Three-case SOC rule of cones.c:21-47 for one element.
+template <typename T>
+__device__ __forceinline__ T soc_rule(T v, bool is_head, T head, T tail) {
+  if (tail <= head) return v;
+  if (tail <= -head) return T(0);
+  const T half = (tail + head) / T(2);
+  return is_head ? half : half * v / tail;
+}
+
+template <typename T, int BLOCK>
+__device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int iter_cap, T *g1,
+                               T *g2, T *tt, T *pbuf, double *scratch) {
+  const int tid = threadIdx.x;
+  const int m = I.m, n = I.n, f = I.f, l = I.l;
+  T *x = B.x + I.col0, *q = B.q + I.col0;
+  T *s = B.s + I.row0, *y = B.y + I.row0, *st = B.st + I.row0, *u = B.u + I.row0,
+    *ax = B.ax + I.row0;
+  const T *b = B.b + I.row0, *D = B.D + I.row0, *c = B.c + I.col0, *E = B.E + I.col0;
+  const T lam = (T)I.lambda;
+  const T alpha = (T)I.alpha, oma = (T)(1.0 - I.alpha);
+
+  State S = *gst;  // every thread keeps its own copy of the scalars
+  if (S.done) return;
+
+  // Dual update of one finished row and the next iteration's residual inputs
+  // (pdos.c:232-236, linAlg.h:158-175, indirect/private.c:20-29, :58-60).
+  auto finish = [&](int r, T sv, T stv, T axv, double &pr2, double &byv) {
+    const T yv = y[r] + (sv - stv) / lam;
+    y[r] = yv;
+    s[r] = sv;
+    const T bv = b[r];
+    const T pr = ((sv - bv) + axv) / D[r];
+    pr2 += (double)pr * (double)pr;
+    u[r] = ((sv + lam * yv) - bv) + axv;
+    byv += (double)bv * (double)yv;
+  };
+
+  if (!S.prepped) {  // A x0: residual, u and b'y of iteration 0
+    for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
+    __syncthreads();
+    double red[2] = {0.0, 0.0};
+    hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int r, T a, T) {
+      ax[r] = a;
+      const T sv = s[r], bv = b[r], yv = y[r];
+      const T pr = ((sv - bv) + a) / D[r];
+      red[0] += (double)pr * (double)pr;
+      u[r] = ((sv + lam * yv) - bv) + a;
+      red[1] += (double)bv * (double)yv;
+    });
+    block_sum_n<BLOCK, 2>(red, scratch);
+    S.pres_sq = red[0];
+    S.by = red[1];
+    S.prepped = 1;
+  }
+
+  bool newly_done = false;
+  for (int it = 0; it < iter_cap; ++it) {
+    // ---- top: A' on (y, u): dual residual, c'x, CG start; stop test
+    for (int r = tid; r < m; r += BLOCK) {
+      g1[r] = y[r];
+      g2[r] = u[r];
+    }
+    __syncthreads();
+    double top[3] = {0.0, 0.0, 0.0};
+    hyb_product<T, BLOCK, 2>(B.At, I.At, g1, g2, pbuf, [&](int j, T sy, T su) {
+      const T cj = c[j];
+      const T dr = (cj + sy) / E[j];
+      top[0] += (double)dr * (double)dr;
+      top[1] += (double)cj * (double)x[j];
+      const T qj = (-lam) * cj + (-su);
+      q[j] = qj;
+      top[2] += (double)qj * (double)qj;
+    });
+    block_sum_n<BLOCK, 3>(top, scratch);
+    S.p_res = sqrt(S.pres_sq);
+    S.d_res = sqrt(top[0]);
+    S.p_obj = top[1];
+    S.d_obj = -S.by;
+    S.eta = fabs(S.p_obj - S.d_obj);
+    if (S.p_res < I.eps * I.pscale && S.d_res < I.eps * I.dscale &&
+        S.eta < I.eps * (1.0 + fabs(S.p_obj) + fabs(S.d_obj))) {
+      S.solved = 1;
+      S.done = 1;
+      newly_done = true;
+      break;
+    }
+    // ---- CG on (I + A'A) x = ... warm-started at x (indirect/private.c:31-104)
+    double qsold = top[2];
+    int cg_iter = 0;
+    bool active = I.cg_max > 0 && qsold > I.tol_sq;
+    if (active) {
+      for (int j = tid; j < n; j += BLOCK) g1[j] = q[j];  // p = q
+      __syncthreads();
+    }
+    while (active) {
+      hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int r, T a, T) { g2[r] = a; });
+      __syncthreads();
+      double pt[1] = {0.0};
+      hyb_product<T, BLOCK, 1>(B.At, I.At, g2, g2, pbuf, [&](int j, T a, T) {
+        const T pj = g1[j];
+        const T tj = pj + a;
+        tt[j] = tj;
+        pt[0] += (double)pj * (double)tj;
+      });
+      block_sum_n<BLOCK, 1>(pt, scratch);
+      const double step = qsold / pt[0];
+      const T stp = (T)step, nstp = (T)(-step);
+      double qs[1] = {0.0};
+      for (int j = tid; j < n; j += BLOCK) {
+        x[j] = x[j] + stp * g1[j];
+        const T qj = q[j] + nstp * tt[j];
+        q[j] = qj;
+        qs[0] += (double)qj * (double)qj;
+      }
+      block_sum_n<BLOCK, 1>(qs, scratch);
+      ++cg_iter;
+      ++S.cg_total;
+      double ratio = 0.0;
+      if (qs[0] < I.tol_sq) {
+        active = false;
+      } else {
+        ratio = qs[0] / qsold;
+        qsold = qs[0];
+        if (cg_iter >= I.cg_max) active = false;
+      }
+      if (active) {
+        const T beta = (T)ratio;
+        for (int j = tid; j < n; j += BLOCK) g1[j] = beta * g1[j] + q[j];
+        __syncthreads();
+      }
+    }
+    // ---- A x: s~ = b - Ax, relax, s = s~ - lam y; zero / orthant rows done
+    for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
+    __syncthreads();
+    double fin[2] = {0.0, 0.0};
+    hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int r, T a, T) {
+      T stv = b[r] + (-a);
+      stv = alpha * stv + oma * s[r];
+      T v = stv - lam * y[r];
+      ax[r] = a;
+      if (r < f) {
+        finish(r, T(0), stv, a, fin[0], fin[1]);
+      } else if (r < f + l) {
+        if (v < T(0)) v = T(0);
+        finish(r, v, stv, a, fin[0], fin[1]);
+      } else {
+        s[r] = v;
+        st[r] = stv;
+      }
+    });
+    __syncthreads();
+    // ---- second-order cones: a warp per small cone, the CTA per big cone
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+      for (int k = warp; k < I.ncones; k += BLOCK / 32) {
+        const int off = B.cone_off[I.cone0 + k], len = B.cone_len[I.cone0 + k];
+        if (len > kSmallCone) continue;
+        T acc = T(0);
+        for (int i = 1 + lane; i < len; i += 32) {
+          const T v = s[off + i];
+          acc += v * v;
+        }
+        acc = warp_sum_t(acc);
+        const T tail = sqrt(acc);
+        const T head = s[off];
+        __syncwarp();
+        for (int i = lane; i < len; i += 32) {
+          const int r = off + i;
+          finish(r, soc_rule(s[r], i == 0, head, tail), st[r], ax[r], fin[0], fin[1]);
+        }
+      }
+      for (int k = 0; k < I.ncones; ++k) {  // uniform over the CTA
+        const int off = B.cone_off[I.cone0 + k], len = B.cone_len[I.cone0 + k];
+        if (len <= kSmallCone) continue;
+        const T head = s[off];  // read before any thread rewrites the cone
+        double acc[1] = {0.0};
+        for (int i = 1 + tid; i < len; i += BLOCK) {
+          const T v = s[off + i];
+          acc[0] += (double)(v * v);
+        }
+        block_sum_n<BLOCK, 1>(acc, scratch);
+        const T tail = (T)sqrt(acc[0]);
+        for (int i = tid; i < len; i += BLOCK) {
+          const int r = off + i;
+          finish(r, soc_rule(s[r], i == 0, head, tail), st[r], ax[r], fin[0], fin[1]);
+        }
+      }
+    }
+    block_sum_n<BLOCK, 2>(fin, scratch);
+    S.pres_sq = fin[0];
+    S.by = fin[1];
+    S.admm_iter += 1;
+    if (S.admm_iter >= I.max_iters) {
+      S.done = 1;
+      newly_done = true;
+      break;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    *gst = S;
+    if (newly_done) atomicAdd(B.ndone, 1);
+  }
+}
+
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1) batch_admm_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double scratch[3 * (BLOCK / 32)];
+  __shared__ Inst s_inst;
+  __shared__ int s_k;
+  T *g1 = reinterpret_cast<T *>(smem_raw);
+  T *g2 = g1 + sm.g1;
+  T *tt = g2 + sm.g2;
+  T *pbuf = tt + sm.tt;
+  const int begin = B.class_begin[cls], count = B.class_begin[cls + 1] - begin;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_k = atomicAdd(&B.queue[cls], 1);
+    __syncthreads();
+    const int k = s_k;
+    if (k >= count) break;
+    const int id = B.order[begin + k];
+    if (threadIdx.x < (int)(sizeof(Inst) / 4))
+      reinterpret_cast<int32_t *>(&s_inst)[threadIdx.x] =
+          reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
+    __syncthreads();
+    solve_instance<T, BLOCK>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch);
+  }
+}
+
+static_assert(sizeof(Inst) % 4 == 0 && sizeof(Inst) / 4 <= 128, "Inst is copied by one 128-thread pass");
+
+// y = D y-unscale etc. (pdos.c:261-294) over the stacked vectors.
+template <typename T>
+__global__ void unscale_kernel(const T *x, const T *s, const T *y, const double *D, const double *E,
+                               int64_t n, int64_t m, double *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n + m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < n) {
+      out[i] = E[i] * (double)x[i];
+    } else {
+      const int64_t r = i - n;
+      out[n + r] = (double)s[r] / D[r];
+      out[n + m + r] = D[r] * (double)y[r];
+    }
+  }
+}
+
+// Warm start from device arrays (unscaled, stacked): the scaling of
+// common.h:147-161 and the x-space ratio of common.h:185-192.
+template <typename T>
+__global__ void warm_start_kernel(const double *x0, const double *y0, const double *s0,
+                                  const double *D, const double *Epre, int64_t n, int64_t m,
+                                  T *xi, T *yi, T *si) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n + m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < n) {
+      if (x0) xi[i] = (T)((x0[i] / Epre[i]) / 1e3);
+    } else {
+      const int64_t r = i - n;
+      if (y0) yi[r] = (T)(y0[r] / D[r]);
+      if (s0) si[r] = (T)(s0[r] * D[r]);
+    }
+  }
+}
+
+template <typename T>
+__global__ void gather_values_kernel(const int32_t *src, int64_t count, const T *from, T *to) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = src[i];
+    to[i] = p >= 0 ? from[p] : T(0);
+  }
+}
+
+// ------------------------------------------------------------ host side
+struct HybBuild {
+  std::vector<int64_t> slice_beg;
+  std::vector<int32_t> slice_w;
+  std::vector<uint32_t> slice_skip;
+  std::vector<int32_t> piece_row, piece_len, split_row, split_p0, split_np;
+  std::vector<int64_t> piece_beg;
+  std::vector<int32_t> idx, src;  // per element: local gather index, source position
+
+  // Rows [r0, r1) of a row-wise matrix (ptr, gidx absolute); gather indices
+  // are made local by subtracting c0.
+  Side add(const int32_t *ptr, const int32_t *gidx, int64_t r0, int64_t r1, int64_t c0) {
+    Side sd{};
+    const int64_t R = r1 - r0;
+    sd.rows = (int32_t)R;
+    sd.slice0 = (int64_t)slice_skip.size();
+    sd.piece0 = (int64_t)piece_row.size();
+    sd.split0 = (int64_t)split_row.size();
+    for (int64_t s0 = 0; s0 < R; s0 += 32) {
+      uint32_t skip = 0;
+      int width = 0;
+      for (int lane = 0; lane < 32; ++lane) {
+        const int64_t r = s0 + lane;
+        if (r >= R) {
+          skip |= 1u << lane;
+          continue;
+        }
+        const int len = ptr[r0 + r + 1] - ptr[r0 + r];
+        if (len > kLongRow) {
+          skip |= 1u << lane;
+          continue;
+        }
+        width = std::max(width, len);
+      }
+      slice_beg.push_back((int64_t)idx.size());
+      slice_w.push_back(width);
+      for (int cidx = 0; cidx < width; ++cidx) {
+        for (int lane = 0; lane < 32; ++lane) {
+          const int64_t r = s0 + lane;
+          int32_t j = 0, p = -1;
+          if (!((skip >> lane) & 1u)) {
+            const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
+            if (cidx < len) {
+              p = (int32_t)(a + cidx);
+              j = (int32_t)(gidx[a + cidx] - c0);
+            }
+          }
+          idx.push_back(j);
+          src.push_back(p);
+        }
+      }
+      slice_skip.push_back(skip);
+      ++sd.nslices;
+    }
+    for (int64_t r = 0; r < R; ++r) {
+      const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
+      if (len <= kLongRow) continue;
+      const int64_t np = (len + kPiece - 1) / kPiece;
+      if (np > 1) {
+        split_row.push_back((int32_t)r);
+        split_p0.push_back((int32_t)((int64_t)piece_row.size() - sd.piece0));
+        split_np.push_back((int32_t)np);
+        ++sd.nsplit;
+      }
+      for (int64_t k = 0; k < np; ++k) {  // nearly equal pieces
+        const int64_t e0 = a + len * k / np, e1 = a + len * (k + 1) / np;
+        piece_row.push_back(np > 1 ? ~(int32_t)r : (int32_t)r);
+        piece_beg.push_back((int64_t)idx.size());
+        piece_len.push_back((int32_t)(e1 - e0));
+        for (int64_t e = e0; e < e1; ++e) {
+          idx.push_back((int32_t)(gidx[e] - c0));
+          src.push_back((int32_t)e);
+        }
+        ++sd.npieces;
+      }
+    }
+    // pad to a multiple of 4 elements so that the next instance starts aligned
+    while (idx.size() % 4) {
+      idx.push_back(0);
+      src.push_back(-1);
+    }
+    return sd;
+  }
+};
+
+template <typename T>
+struct HybDevOwned {
+  Hyb<T> h{};
+  int upload(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStream_t st) {
+    auto up = [&](auto **dst, const auto &v) -> int {
+      using E = typename std::decay_t<decltype(v)>::value_type;
+      E *p = nullptr;
+      PDOS_TRY(arena.alloc(&p, v.size() + 1));
+      if (!v.empty())
+        PDOS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice, st));
+      *dst = p;
+      return PDOSGPU_OK;
+    };
+    int64_t *slice_beg, *piece_beg;
+    uint32_t *slice_skip;
+    int32_t *slice_w, *piece_row, *piece_len, *split_row, *split_p0, *split_np, *idx;
+    PDOS_TRY(up(&slice_beg, hb.slice_beg));
+    PDOS_TRY(up(&slice_w, hb.slice_w));
+    PDOS_TRY(up(&slice_skip, hb.slice_skip));
+    PDOS_TRY(up(&piece_row, hb.piece_row));
+    PDOS_TRY(up(&piece_beg, hb.piece_beg));
+    PDOS_TRY(up(&piece_len, hb.piece_len));
+    PDOS_TRY(up(&split_row, hb.split_row));
+    PDOS_TRY(up(&split_p0, hb.split_p0));
+    PDOS_TRY(up(&split_np, hb.split_np));
+    PDOS_TRY(up(&idx, hb.idx));
+    T *val = nullptr;
+    PDOS_TRY(arena.alloc(&val, hb.src.size() + 1));
+    if (!hb.src.empty()) {
+      DeviceArena tmp;
+      int32_t *src = nullptr;
+      PDOS_TRY(tmp.alloc(&src, hb.src.size()));
+      PDOS_CUDA_TRY(cudaMemcpyAsync(src, hb.src.data(), sizeof(int32_t) * hb.src.size(),
+                                    cudaMemcpyHostToDevice, st));
+      const int64_t cnt = (int64_t)hb.src.size();
+      const int g = (int)std::min<int64_t>((cnt + 255) / 256, (int64_t)num_sms() * 16);
+      gather_values_kernel<T><<<g, 256, 0, st>>>(src, cnt, values, val);
+      PDOS_CUDA_TRY(cudaGetLastError());
+      PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before src is freed
+    }
+    h = Hyb<T>{slice_beg, slice_w, slice_skip, piece_row, piece_beg, piece_len, split_row, split_p0,
+               split_np, idx, val};
+    return PDOSGPU_OK;
+  }
+};
+
+inline double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+class BatchBase {
+ public:
+  virtual ~BatchBase() {}
+  virtual int solve(int64_t max_launches) = 0;
+  virtual int reset() = 0;
+  virtual int warm_start(const double *x0, const double *y0, const double *s0) = 0;
+  virtual int fetch(int64_t first, int64_t count, double *x, double *s, double *y,
+                    pdosgpu_info *info) = 0;
+  virtual int tune(int iters, int *blocks_out) = 0;
+  virtual int set_blocks(const int *blocks) = 0;
+  virtual void *stream() = 0;
+  virtual int64_t done_count() = 0;
+  int64_t count = 0, total_n = 0, total_m = 0, total_nnz = 0;
+  double setup_ms = 0, solve_ms = 0;
+  int64_t launches = 0;
+  std::vector<int64_t> row0, col0;
+};
+
+template <typename T>
+class BatchEngine : public BatchBase {
+ public:
+  ~BatchEngine() override {
+    for (auto e : exec_)
+      if (e) cudaGraphExecDestroy(e);
+    for (auto e : ev_) if (e) cudaEventDestroy(e);
+    for (auto s : side_) {
+      if (s) cudaStreamDestroy(s);
+    }
+    if (stream_) {
+      cudaStreamSynchronize(stream_);
+      cudaStreamDestroy(stream_);
+    }
+    if (host_done_) cudaFreeHost(host_done_);
+  }
+
+  int setup(const pdosgpu_problem *probs, int64_t count_in, const pdosgpu_options &opt, int iter_cap);
+  int solve(int64_t max_launches) override;
+  int reset() override;
+  int warm_start(const double *x0, const double *y0, const double *s0) override;
+  int fetch(int64_t first, int64_t cnt, double *x, double *s, double *y, pdosgpu_info *info) override;
+  int tune(int iters, int *blocks_out) override;
+  int set_blocks(const int *blocks) override;
+  void *stream() override { return stream_; }
+  int64_t done_count() override;
+
+ private:
+  int build_graph(int iter_cap, cudaGraphExec_t *exec);
+  int configure(int cls, int block);
+  int launch_class(int cls, int block, int iter_cap, cudaStream_t st);
+  int grid_[kClasses]{};
+  int64_t active_launch_nodes_ = 0;
+
+  DeviceArena arena_;
+  cudaStream_t stream_ = nullptr;
+  std::vector<cudaStream_t> side_;
+  std::vector<cudaEvent_t> ev_;
+  std::vector<cudaGraphExec_t> exec_;  // [0]: one launch of iter_cap iterations
+  int iter_cap_ = 64;
+  Dev<T> dev_{};
+  HybDevOwned<T> hA_, hT_;
+  Inst *inst_d_ = nullptr;
+  State *state_d_ = nullptr;
+  int32_t *queue_ = nullptr, *ndone_ = nullptr;
+  int32_t *host_done_ = nullptr;
+  std::vector<Inst> inst_h_;
+  std::vector<int32_t> class_begin_h_;
+  Smem smem_[kClasses]{};
+  int block_[kClasses]{};
+  T *x_init_ = nullptr, *y_init_ = nullptr, *s_init_ = nullptr;
+  double *D64_ = nullptr, *E64_ = nullptr, *Epre64_ = nullptr, *out_ = nullptr;
+  double *warm_[3] = {nullptr, nullptr, nullptr};
+};
+
+template <typename T>
+int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosgpu_options &opt,
+                          int iter_cap) {
+  const double t0 = now_ms();
+  if (cnt <= 0 || cnt > (int64_t)INT32_MAX / 2) return fail(PDOSGPU_EINVAL, "batch count out of range");
+  if (iter_cap <= 0) return fail(PDOSGPU_EINVAL, "iterations per launch must be positive");
+  iter_cap_ = iter_cap;
+  count = cnt;
+  int64_t N = 0, M = 0, NNZ = 0, ncones = 0;
+  bool any_x = false, any_y = false, any_s = false;
+  for (int64_t i = 0; i < cnt; ++i) {
+    const pdosgpu_problem &p = probs[i];
+    const int rc = validate_problem(p);
+    if (rc != PDOSGPU_OK) return fail(rc, "instance " + std::to_string(i) + ": " + pdos_gpu_last_error());
+    if ((p.normalize != 0) != (probs[0].normalize != 0))
+      return fail(PDOSGPU_EINVAL, "all instances of a batch must share NORMALIZE");
+    if (p.verbose) {
+      // the batch prints nothing per iteration
+    }
+    row0.push_back(M);
+    col0.push_back(N);
+    N += p.n;
+    M += p.m;
+    NNZ += p.Ap[p.n];
+    ncones += p.qsize;
+    any_x |= p.x0 != nullptr;
+    any_y |= p.y0 != nullptr;
+    any_s |= p.s0 != nullptr;
+  }
+  row0.push_back(M);
+  col0.push_back(N);
+  const int64_t lim = (int64_t)INT32_MAX - 4096;
+  if (N > lim || M > lim || NNZ > lim)
+    return fail(PDOSGPU_EINVAL, "stacked m, n and nnz must each be below 2^31 - 4096");
+  if (probs[0].normalize && opt.scaling == PDOSGPU_SCALE_RUIZ)
+    return fail(PDOSGPU_ENOTSUP, "Ruiz equilibration is not available for batches");
+  total_n = N;
+  total_m = M;
+  total_nnz = NNZ;
+
+  // ---- stacked problem (block diagonal), host
+  std::vector<double> Ax(NNZ), b(M), c(N), x0, y0, s0;
+  std::vector<int64_t> Ai(NNZ), Ap(N + 1);
+  if (any_x) x0.assign(N, 0.0);
+  if (any_y) y0.assign(M, 0.0);
+  if (any_s) s0.assign(M, 0.0);
+  ProblemDesc d;
+  {
+    int64_t e = 0;
+    for (int64_t i = 0; i < cnt; ++i) {
+      const pdosgpu_problem &p = probs[i];
+      const int64_t nz = p.Ap[p.n];
+      for (int64_t j = 0; j < p.n; ++j) Ap[col0[i] + j] = e + p.Ap[j];
+      if (nz > 0) std::memcpy(&Ax[e], p.Ax, sizeof(double) * nz);
+      for (int64_t k = 0; k < nz; ++k) Ai[e + k] = row0[i] + p.Ai[k];
+      e += nz;
+      std::memcpy(&b[row0[i]], p.b, sizeof(double) * p.m);
+      std::memcpy(&c[col0[i]], p.c, sizeof(double) * p.n);
+      if (p.x0) std::memcpy(&x0[col0[i]], p.x0, sizeof(double) * p.n);
+      if (p.y0) std::memcpy(&y0[row0[i]], p.y0, sizeof(double) * p.m);
+      if (p.s0) std::memcpy(&s0[row0[i]], p.s0, sizeof(double) * p.m);
+      int64_t off = row0[i] + p.f + p.l;
+      for (int64_t k = 0; k < p.qsize; ++k) {
+        d.soc_off.push_back(off);
+        d.soc_len.push_back(p.q[k]);
+        off += p.q[k];
+      }
+    }
+    Ap[N] = e;
+  }
+  d.n = N;
+  d.m = M;
+  d.nnz = NNZ;
+  d.Ax = Ax.data();
+  d.Ai = Ai.data();
+  d.Ap = Ap.data();
+  d.b = b.data();
+  d.c = c.data();
+  d.x0 = any_x ? x0.data() : nullptr;
+  d.y0 = any_y ? y0.data() : nullptr;
+  d.s0 = any_s ? s0.data() : nullptr;
+  d.inst_row0 = row0;
+  d.inst_col0 = col0;
+  d.normalize = probs[0].normalize ? 1 : 0;
+
+  PDOS_CUDA_TRY(cudaSetDevice(opt.device));
+  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  cudaStream_t st = stream_;
+  DeviceProblem<T> P;
+  PDOS_TRY(setup_problem<T>(d, arena_, st, P));
+  D64_ = P.D64;
+  E64_ = P.E64;
+  Epre64_ = P.Epre64;
+  x_init_ = P.x_init;
+  y_init_ = P.y_init;
+  s_init_ = P.s_init;
+
+  // ---- hybrid layouts of both sides, instance by instance
+  std::vector<int32_t> Rj(NNZ > 0 ? NNZ : 1), ApI(N + 1);
+  if (NNZ > 0)
+    PDOS_CUDA_TRY(cudaMemcpyAsync(Rj.data(), P.Rj, sizeof(int32_t) * NNZ, cudaMemcpyDeviceToHost, st));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int32_t> AiI(NNZ > 0 ? NNZ : 1);
+  for (int64_t k = 0; k < NNZ; ++k) AiI[k] = (int32_t)Ai[k];
+  HybBuild bA, bT;
+  inst_h_.assign(cnt, Inst{});
+  std::vector<int32_t> cone_off_h, cone_len_h;
+  int64_t cone_pos = 0;
+  for (int64_t i = 0; i < cnt; ++i) {
+    const pdosgpu_problem &p = probs[i];
+    Inst &I = inst_h_[i];
+    I.row0 = row0[i];
+    I.col0 = col0[i];
+    I.m = (int32_t)p.m;
+    I.n = (int32_t)p.n;
+    I.f = (int32_t)p.f;
+    I.l = (int32_t)p.l;
+    I.cone0 = cone_pos;
+    I.ncones = (int32_t)p.qsize;
+    int64_t off = p.f + p.l;
+    for (int64_t k = 0; k < p.qsize; ++k) {
+      cone_off_h.push_back((int32_t)off);
+      cone_len_h.push_back((int32_t)p.q[k]);
+      off += p.q[k];
+    }
+    cone_pos += p.qsize;
+    I.A = bA.add(P.rp_host.data(), Rj.data(), row0[i], row0[i + 1], col0[i]);
+    I.At = bT.add(P.ap_host.data(), AiI.data(), col0[i], col0[i + 1], row0[i]);
+    I.lambda = P.lambda[i];
+    I.pscale = P.pscale[i];
+    I.dscale = P.dscale[i];
+    I.alpha = p.alpha;
+    I.eps = p.eps_abs;
+    I.tol_sq = p.cg_tol * p.cg_tol;
+    I.max_iters = p.max_iters;
+    I.cg_max = p.cg_max_its;
+    const int64_t nz = p.Ap[p.n];
+    int cls = 0;
+    while (cls < kClasses - 1 && nz > kClassNnz[cls]) ++cls;
+    I.cls = cls;
+  }
+  PDOS_TRY(hA_.upload(bA, P.Rx, arena_, st));
+  PDOS_TRY(hT_.upload(bT, P.Ax, arena_, st));
+
+  // ---- classes: shared-memory regions and the processing order (largest
+  // instances first within a class)
+  std::vector<std::vector<int32_t>> members(kClasses);
+  for (int64_t i = 0; i < cnt; ++i) members[inst_h_[i].cls].push_back((int32_t)i);
+  std::vector<int32_t> order;
+  class_begin_h_.assign(kClasses + 1, 0);
+  for (int k = 0; k < kClasses; ++k) {
+    auto &mv = members[k];
+    std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) {
+      return probs[a].Ap[probs[a].n] > probs[bb].Ap[probs[bb].n];
+    });
+    Smem sm{0, 0, 0, 0};
+    for (int32_t i : mv) {
+      const Inst &I = inst_h_[i];
+      sm.g1 = std::max(sm.g1, std::max(I.m, I.n));
+      sm.g2 = std::max(sm.g2, I.m);
+      sm.tt = std::max(sm.tt, I.n);
+      sm.pb = std::max(sm.pb, 2 * std::max(I.A.npieces, I.At.npieces));
+    }
+    auto r4 = [](int32_t v) { return (v + 3) & ~3; };
+    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb)};
+    if (sm.bytes(sizeof(T)) > (size_t)kSmemLimit)
+      return fail(PDOSGPU_ENOTSUP, "an instance of the batch is too large for one CTA's shared memory "
+                                   "(max(m, n) + m + n + pieces above " +
+                                   std::to_string(kSmemLimit / sizeof(T)) +
+                                   " values); solve it with pdosgpu_setup");
+    smem_[k] = sm;
+    block_[k] = k == 0 ? 128 : (k == 1 ? 256 : 512);
+    order.insert(order.end(), mv.begin(), mv.end());
+    class_begin_h_[k + 1] = (int32_t)order.size();
+  }
+
+  // ---- device arrays
+  int32_t *order_d, *class_begin_d, *cone_off_d, *cone_len_d;
+  PDOS_TRY(arena_.alloc(&inst_d_, (size_t)cnt));
+  PDOS_TRY(arena_.alloc(&state_d_, (size_t)cnt));
+  PDOS_TRY(arena_.alloc(&order_d, order.size()));
+  PDOS_TRY(arena_.alloc(&class_begin_d, (size_t)kClasses + 1));
+  PDOS_TRY(arena_.alloc(&queue_, (size_t)kClasses + 1));
+  ndone_ = queue_ + kClasses;
+  PDOS_TRY(arena_.alloc(&cone_off_d, cone_off_h.size() + 1));
+  PDOS_TRY(arena_.alloc(&cone_len_d, cone_len_h.size() + 1));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(inst_d_, inst_h_.data(), sizeof(Inst) * cnt, cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(order_d, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(class_begin_d, class_begin_h_.data(), sizeof(int32_t) * (kClasses + 1),
+                                cudaMemcpyHostToDevice, st));
+  if (!cone_off_h.empty()) {
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_off_d, cone_off_h.data(), sizeof(int32_t) * cone_off_h.size(),
+                                  cudaMemcpyHostToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_len_d, cone_len_h.data(), sizeof(int32_t) * cone_len_h.size(),
+                                  cudaMemcpyHostToDevice, st));
+  }
+  Dev<T> &B = dev_;
+  B.inst = inst_d_;
+  B.state = state_d_;
+  B.order = order_d;
+  B.class_begin = class_begin_d;
+  B.queue = queue_;
+  B.ndone = ndone_;
+  PDOS_TRY(arena_.alloc(&B.x, (size_t)N));
+  PDOS_TRY(arena_.alloc(&B.q, (size_t)N));
+  PDOS_TRY(arena_.alloc(&B.s, (size_t)M));
+  PDOS_TRY(arena_.alloc(&B.y, (size_t)M));
+  PDOS_TRY(arena_.alloc(&B.st, (size_t)M));
+  PDOS_TRY(arena_.alloc(&B.u, (size_t)M));
+  PDOS_TRY(arena_.alloc(&B.ax, (size_t)M));
+  B.b = P.b;
+  B.c = P.c;
+  B.D = P.D;
+  B.E = P.E;
+  B.A = hA_.h;
+  B.At = hT_.h;
+  B.cone_off = cone_off_d;
+  B.cone_len = cone_len_d;
+  PDOS_TRY(arena_.alloc(&out_, (size_t)N + 2 * (size_t)M));
+  PDOS_CUDA_TRY(cudaMallocHost(&host_done_, sizeof(int32_t)));
+
+  for (int k = 0; k < kClasses; ++k) {
+    cudaStream_t s = nullptr;
+    cudaEvent_t e = nullptr;
+    PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    side_.push_back(s);
+    PDOS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ev_.push_back(e);
+  }
+  {
+    cudaEvent_t e = nullptr;
+    PDOS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ev_.push_back(e);  // fork event
+  }
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  PDOS_TRY(reset());
+  exec_.assign(1, nullptr);
+  PDOS_TRY(build_graph(iter_cap_, &exec_[0]));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  setup_ms = now_ms() - t0;
+  return PDOSGPU_OK;
+}
+
+// Kernel attributes and grid of one class at one CTA size (outside any
+// stream capture).
+template <typename T>
+int BatchEngine<T>::configure(int cls, int block) {
+  const size_t bytes = smem_[cls].bytes(sizeof(T));
+  auto go = [&](auto kernel) -> int {
+    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    int per_sm = 0;
+    PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, bytes));
+    if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "batch kernel does not fit on an SM");
+    const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
+    grid_[cls] = std::max(1, std::min(members, per_sm * num_sms()));
+    return PDOSGPU_OK;
+  };
+  switch (block) {
+    case 128: return go(batch_admm_kernel<T, 128>);
+    case 256: return go(batch_admm_kernel<T, 256>);
+    case 512: return go(batch_admm_kernel<T, 512>);
+    default: return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+  }
+}
+
+template <typename T>
+int BatchEngine<T>::launch_class(int cls, int block, int iter_cap, cudaStream_t st) {
+  const Smem sm = smem_[cls];
+  const size_t bytes = sm.bytes(sizeof(T));
+  switch (block) {
+    case 128: batch_admm_kernel<T, 128><<<grid_[cls], 128, bytes, st>>>(dev_, cls, sm, iter_cap); break;
+    case 256: batch_admm_kernel<T, 256><<<grid_[cls], 256, bytes, st>>>(dev_, cls, sm, iter_cap); break;
+    case 512: batch_admm_kernel<T, 512><<<grid_[cls], 512, bytes, st>>>(dev_, cls, sm, iter_cap); break;
+    default: return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+  }
+  PDOS_CUDA_TRY(cudaGetLastError());
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int BatchEngine<T>::build_graph(int iter_cap, cudaGraphExec_t *exec) {
+  cudaStream_t st = stream_;
+  for (int k = 0; k < kClasses; ++k)
+    if (class_begin_h_[k + 1] > class_begin_h_[k]) PDOS_TRY(configure(k, block_[k]));
+  cudaGraph_t graph = nullptr;
+  PDOS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int rc = PDOSGPU_OK;
+  int64_t nodes = 1;
+  do {
+    if (cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st) != cudaSuccess) {
+      rc = fail(PDOSGPU_ECUDA, "queue reset");
+      break;
+    }
+    if (cudaEventRecord(ev_[kClasses], st) != cudaSuccess) {
+      rc = fail(PDOSGPU_ECUDA, "graph fork");
+      break;
+    }
+    for (int k = 0; k < kClasses && rc == PDOSGPU_OK; ++k) {
+      if (class_begin_h_[k + 1] == class_begin_h_[k]) continue;
+      if (cudaStreamWaitEvent(side_[k], ev_[kClasses], 0) != cudaSuccess) {
+        rc = fail(PDOSGPU_ECUDA, "graph fork");
+        break;
+      }
+      rc = launch_class(k, block_[k], iter_cap, side_[k]);
+      if (rc != PDOSGPU_OK) break;
+      ++nodes;
+      if (cudaEventRecord(ev_[k], side_[k]) != cudaSuccess || cudaStreamWaitEvent(st, ev_[k], 0) != cudaSuccess)
+        rc = fail(PDOSGPU_ECUDA, "graph join");
+    }
+  } while (0);
+  cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (rc != PDOSGPU_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(PDOSGPU_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(PDOSGPU_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  active_launch_nodes_ = nodes - 1;
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int BatchEngine<T>::reset() {
+  cudaStream_t st = stream_;
+  const Dev<T> &B = dev_;
+  PDOS_CUDA_TRY(cudaMemcpyAsync(B.x, x_init_, sizeof(T) * total_n, cudaMemcpyDeviceToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(B.y, y_init_, sizeof(T) * total_m, cudaMemcpyDeviceToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(B.s, s_init_, sizeof(T) * total_m, cudaMemcpyDeviceToDevice, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(B.q, 0, sizeof(T) * total_n, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(B.st, 0, sizeof(T) * total_m, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(B.u, 0, sizeof(T) * total_m, st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(B.ax, 0, sizeof(T) * total_m, st));
+  std::vector<State> h(count);
+  int32_t done = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    State &s = h[i];
+    std::memset(&s, 0, sizeof(s));
+    s.p_res = s.d_res = s.p_obj = s.d_obj = s.eta = -1.0;
+    s.done = inst_h_[i].max_iters <= 0 ? 1 : 0;
+    done += s.done;
+  }
+  PDOS_CUDA_TRY(cudaMemcpyAsync(state_d_, h.data(), sizeof(State) * count, cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(ndone_, &done, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // h and done are host stack memory
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int BatchEngine<T>::warm_start(const double *x0, const double *y0, const double *s0) {
+  cudaStream_t st = stream_;
+  const int64_t len = total_n + total_m;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((len + 255) / 256, (int64_t)num_sms() * 16));
+  warm_start_kernel<T><<<g, 256, 0, st>>>(x0, y0, s0, D64_, Epre64_, total_n, total_m, x_init_, y_init_,
+                                          s_init_);
+  PDOS_CUDA_TRY(cudaGetLastError());
+  return reset();
+}
+
+template <typename T>
+int64_t BatchEngine<T>::done_count() {
+  if (cudaMemcpyAsync(host_done_, ndone_, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_) != cudaSuccess)
+    return -1;
+  if (cudaStreamSynchronize(stream_) != cudaSuccess) return -1;
+  return *host_done_;
+}
+
+template <typename T>
+int BatchEngine<T>::solve(int64_t max_launches) {
+  const double t0 = now_ms();
+  int64_t launched = 0;
+  int64_t between = 1;  // launches queued between two reads of the done count
+  int64_t done = done_count();
+  if (done < 0) return fail(PDOSGPU_ECUDA, "reading the batch state failed");
+  while (done < count && (max_launches < 0 || launched < max_launches)) {
+    int64_t nb = between;
+    if (max_launches >= 0) nb = std::min<int64_t>(nb, max_launches - launched);
+    for (int64_t k = 0; k < nb; ++k) {
+      PDOS_CUDA_TRY(cudaGraphLaunch(exec_[0], stream_));
+      launches += active_launch_nodes_;
+    }
+    launched += nb;
+    done = done_count();
+    if (done < 0) return fail(PDOSGPU_ECUDA, "reading the batch state failed");
+    if (between < 4) between *= 2;
+  }
+  PDOS_CUDA_TRY(cudaStreamSynchronize(stream_));
+  solve_ms = now_ms() - t0;
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int BatchEngine<T>::fetch(int64_t first, int64_t cnt, double *x, double *s, double *y,
+                          pdosgpu_info *info) {
+  if (first < 0 || cnt < 0 || first + cnt > count) return fail(PDOSGPU_EINVAL, "instance range out of bounds");
+  if (cnt == 0) return PDOSGPU_OK;
+  cudaStream_t st = stream_;
+  const Dev<T> &B = dev_;
+  const int64_t n = total_n, m = total_m;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + m + 255) / 256, (int64_t)num_sms() * 16));
+  unscale_kernel<T><<<g, 256, 0, st>>>(B.x, B.s, B.y, D64_, E64_, n, m, out_);
+  PDOS_CUDA_TRY(cudaGetLastError());
+  const int64_t c0 = col0[first], c1 = col0[first + cnt], r0 = row0[first], r1 = row0[first + cnt];
+  if (x) PDOS_CUDA_TRY(cudaMemcpyAsync(x, out_ + c0, sizeof(double) * (c1 - c0), cudaMemcpyDeviceToHost, st));
+  if (s) PDOS_CUDA_TRY(cudaMemcpyAsync(s, out_ + n + r0, sizeof(double) * (r1 - r0), cudaMemcpyDeviceToHost, st));
+  if (y) PDOS_CUDA_TRY(cudaMemcpyAsync(y, out_ + n + m + r0, sizeof(double) * (r1 - r0), cudaMemcpyDeviceToHost, st));
+  std::vector<State> h(cnt);
+  PDOS_CUDA_TRY(cudaMemcpyAsync(h.data(), state_d_ + first, sizeof(State) * cnt, cudaMemcpyDeviceToHost, st));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  if (info) {
+    for (int64_t i = 0; i < cnt; ++i) {
+      pdosgpu_info &o = info[i];
+      std::memset(&o, 0, sizeof(o));
+      o.admm_iters = h[i].admm_iter;
+      o.cg_iters = h[i].cg_total;
+      o.solved = h[i].solved;
+      o.p_res = h[i].p_res;
+      o.d_res = h[i].d_res;
+      o.p_obj = h[i].p_obj;
+      o.d_obj = h[i].d_obj;
+      o.eta = h[i].eta;
+      o.lambda = inst_h_[first + i].lambda;
+      o.setup_ms = setup_ms;
+      o.solve_ms = solve_ms;
+      o.kernel_launches = launches;
+    }
+  }
+  return PDOSGPU_OK;
+}
+
+template <typename T>
+int BatchEngine<T>::set_blocks(const int *blocks) {
+  for (int k = 0; k < kClasses; ++k) {
+    bool ok = false;
+    for (int j = 0; j < kNumBlocks; ++j) ok |= blocks[k] == kBlocks[j];
+    if (!ok) return fail(PDOSGPU_EINVAL, "CTA sizes must be 128, 256 or 512");
+  }
+  for (int k = 0; k < kClasses; ++k) block_[k] = blocks[k];
+  if (exec_[0]) cudaGraphExecDestroy(exec_[0]);
+  exec_[0] = nullptr;
+  return build_graph(iter_cap_, &exec_[0]);
+}
+
+// Autotuner: for each size class with members, time `iters` iterations of
+// every instance of the class at each CTA size and keep the fastest; the
+// batch is reset afterwards.
+template <typename T>
+int BatchEngine<T>::tune(int iters, int *blocks_out) {
+  if (iters <= 0) return fail(PDOSGPU_EINVAL, "iters must be positive");
+  cudaStream_t st = stream_;
+  cudaEvent_t e0, e1;
+  PDOS_CUDA_TRY(cudaEventCreate(&e0));
+  PDOS_CUDA_TRY(cudaEventCreate(&e1));
+  int rc = PDOSGPU_OK;
+  for (int k = 0; k < kClasses && rc == PDOSGPU_OK; ++k) {
+    if (class_begin_h_[k + 1] == class_begin_h_[k]) continue;
+    float best = -1.f;
+    for (int j = 0; j < kNumBlocks && rc == PDOSGPU_OK; ++j) {
+      const int blk = kBlocks[j];
+      if (smem_[k].bytes(sizeof(T)) > (size_t)kSmemLimit) continue;
+      rc = reset();
+      if (rc == PDOSGPU_OK) rc = configure(k, blk);
+      if (rc != PDOSGPU_OK) break;
+      // prepare (first pass) outside the timed region
+      if (cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st) != cudaSuccess) {
+        rc = fail(PDOSGPU_ECUDA, "queue reset");
+        break;
+      }
+      rc = launch_class(k, blk, 1, st);
+      if (rc != PDOSGPU_OK) break;
+      cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st);
+      cudaEventRecord(e0, st);
+      rc = launch_class(k, blk, iters, st);
+      cudaEventRecord(e1, st);
+      if (rc != PDOSGPU_OK) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = fail(PDOSGPU_ECUDA, "tuning launch failed");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      launches += 2;
+      if (best < 0.f || ms < best) {
+        best = ms;
+        block_[k] = blk;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  PDOS_TRY(rc);
+  if (blocks_out)
+    for (int k = 0; k < kClasses; ++k) blocks_out[k] = block_[k];
+  PDOS_TRY(reset());
+  if (exec_[0]) cudaGraphExecDestroy(exec_[0]);
+  exec_[0] = nullptr;
+  return build_graph(iter_cap_, &exec_[0]);
+}
+
+}  // namespace batch
+}  // namespace pdosgpu
+
+struct pdosgpu_batch {
+  std::unique_ptr<pdosgpu::batch::BatchBase> engine;
+};
+
+using namespace pdosgpu;
+
+extern "C" {
+
+int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count, const pdosgpu_options *opt,
+                        int iters_per_launch, pdosgpu_batch **out) {
+  if (!probs || !out) return fail(PDOSGPU_EINVAL, "NULL argument");
+  *out = nullptr;
+  int devs = 0;
+  cudaError_t e = cudaGetDeviceCount(&devs);
+  if (e != cudaSuccess || devs == 0)
+    return fail(PDOSGPU_ENOTSUP, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  pdosgpu_options o;
+  pdosgpu_default_options(&o);
+  if (opt) o = *opt;
+  auto w = new (std::nothrow) pdosgpu_batch();
+  if (!w) return fail(PDOSGPU_ENOMEM, "host allocation failed");
+  int rc = PDOSGPU_OK;
+  if (iters_per_launch <= 0) iters_per_launch = 64;
+  if (o.precision == PDOSGPU_FP32) {
+    auto b = std::make_unique<batch::BatchEngine<float>>();
+    rc = b->setup(probs, count, o, iters_per_launch);
+    if (rc == PDOSGPU_OK) w->engine = std::move(b);
+  } else if (o.precision == PDOSGPU_FP64) {
+    auto b = std::make_unique<batch::BatchEngine<double>>();
+    rc = b->setup(probs, count, o, iters_per_launch);
+    if (rc == PDOSGPU_OK) w->engine = std::move(b);
+  } else {
+    rc = fail(PDOSGPU_EINVAL, "unknown precision");
+  }
+  if (rc != PDOSGPU_OK) {
+    delete w;
+    return rc;
+  }
+  *out = w;
+  return PDOSGPU_OK;
+}
+
+int pdosgpu_batch_solve(pdosgpu_batch *b) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->solve(-1);
+}
+
+int pdosgpu_batch_launch(pdosgpu_batch *b, int64_t launches) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  if (launches < 0) return fail(PDOSGPU_EINVAL, "launches must be nonnegative");
+  return b->engine->solve(launches);
+}
+
+int pdosgpu_batch_reset(pdosgpu_batch *b) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->reset();
+}
+
+int pdosgpu_batch_warm_start(pdosgpu_batch *b, const double *x0, const double *y0, const double *s0) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->warm_start(x0, y0, s0);
+}
+
+int pdosgpu_batch_fetch(pdosgpu_batch *b, int64_t first, int64_t count, double *x, double *s,
+                        double *y, pdosgpu_info *info) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->fetch(first, count, x, s, y, info);
+}
+
+int64_t pdosgpu_batch_done(pdosgpu_batch *b) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->done_count();
+}
+
+int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->tune(iters, blocks);
+}
+
+int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks) {
+  if (!b || !b->engine || !blocks) return fail(PDOSGPU_EINVAL, "NULL argument");
+  return b->engine->set_blocks(blocks);
+}
+
+int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m, int64_t *nnz) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  if (count) *count = b->engine->count;
+  if (n) *n = b->engine->total_n;
+  if (m) *m = b->engine->total_m;
+  if (nnz) *nnz = b->engine->total_nnz;
+  return PDOSGPU_OK;
+}
+
+void *pdosgpu_batch_stream(pdosgpu_batch *b) {
+  return (b && b->engine) ? b->engine->stream() : nullptr;
+}
+
+void pdosgpu_batch_free(pdosgpu_batch *b) { delete b; }
+
+}  // extern "C"

@@ -8,6 +8,7 @@
 #include <cstring>
 
 #include "engine.cuh"
+#include "problem.cuh"
 #include "setup_kernels.cuh"
 
 namespace pdosgpu {
@@ -141,7 +142,6 @@ class Engine : public EngineBase {
   int build_graph();
   int run_prep();
   int read_state();
-  int build_cones(const pdosgpu_problem &pr);
 
   // sizes
   int32_t m_ = 0, n_ = 0, nnz_ = 0, f_ = 0, l_ = 0;
@@ -178,11 +178,9 @@ class Engine : public EngineBase {
   int grid_dir_ = 1;
 };
 
-template <typename T>
-int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
-  using namespace setup;
-  const double t0 = now_ms();
-  // ---- host-side validation (pdos.c:61-71, pdosmodule.c:94-311)
+// ======================================================== validation
+// Host-side checks of one problem (pdos.c:61-71, pdosmodule.c:94-311).
+int validate_problem(const pdosgpu_problem &pr) {
   if (pr.n <= 0 || pr.m <= 0) return fail(PDOSGPU_EINVAL, "n and m must be positive");
   if (!pr.Ap || !pr.b || !pr.c) return fail(PDOSGPU_EINVAL, "Ap, b and c must not be NULL");
   const int64_t nnz64 = pr.Ap[pr.n];
@@ -203,32 +201,33 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
     return fail(PDOSGPU_EINVAL, "MAX_ITERS and CG_MAX_ITS must be nonnegative");
   if (!(pr.eps_abs >= 0) || !std::isfinite(pr.alpha) || !(pr.cg_tol >= 0))
     return fail(PDOSGPU_EINVAL, "EPS_ABS, ALPHA and CG_TOL must be finite and nonnegative");
+  return PDOSGPU_OK;
+}
 
-  m_ = (int32_t)pr.m;
-  n_ = (int32_t)pr.n;
-  nnz_ = (int32_t)nnz64;
-  f_ = (int32_t)pr.f;
-  l_ = (int32_t)pr.l;
-  qsize_ = pr.qsize;
-  max_iters_ = pr.max_iters;
-  cg_max_ = pr.cg_max_its;
-  verbose_ = (int)pr.verbose;
-  alpha_ = pr.alpha;
-  eps_ = pr.eps_abs;
-  tol_sq_ = pr.cg_tol * pr.cg_tol;
+// ======================================================== setup_problem
+template <typename T>
+int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, DeviceProblem<T> &P) {
+  using namespace setup;
+  const int m = (int)d.m, n = (int)d.n, nnz = (int)d.nnz;
+  const int64_t ninst = (int64_t)d.inst_row0.size() - 1;
+  const int64_t ncones = (int64_t)d.soc_off.size();
+  if (ninst < 1 || (int64_t)d.inst_col0.size() != ninst + 1)
+    return fail(PDOSGPU_EINVAL, "instance ranges are malformed");
+  if (d.ruiz && ninst != 1) return fail(PDOSGPU_EINVAL, "Ruiz equilibration takes one instance");
+  P.m = m;
+  P.n = n;
+  P.nnz = nnz;
   {  // DIMACS denominators from the caller's b and c (pdos.c:76-77)
-    double sb = 0.0, sc = 0.0;
-    for (int64_t i = 0; i < pr.m; ++i) sb += pr.b[i] * pr.b[i];
-    for (int64_t i = 0; i < pr.n; ++i) sc += pr.c[i] * pr.c[i];
-    pscale_ = 1.0 + std::sqrt(sb);
-    dscale_ = 1.0 + std::sqrt(sc);
+    P.pscale.assign(ninst, 1.0);
+    P.dscale.assign(ninst, 1.0);
+    for (int64_t k = 0; k < ninst; ++k) {
+      double sb = 0.0, sc = 0.0;
+      for (int64_t i = d.inst_row0[k]; i < d.inst_row0[k + 1]; ++i) sb += d.b[i] * d.b[i];
+      for (int64_t j = d.inst_col0[k]; j < d.inst_col0[k + 1]; ++j) sc += d.c[j] * d.c[j];
+      P.pscale[k] = 1.0 + std::sqrt(sb);
+      P.dscale[k] = 1.0 + std::sqrt(sc);
+    }
   }
-
-  PDOS_CUDA_TRY(cudaSetDevice(opt.device));
-  g_num_sms = 0;
-  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-  cudaStream_t st = stream_;
-  const int m = m_, n = n_, nnz = nnz_;
 
   DeviceArena tmp;  // set-up temporaries
   // ---- upload and narrow
@@ -241,27 +240,26 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   PDOS_TRY(tmp.alloc(&b0, (size_t)m));
   PDOS_TRY(tmp.alloc(&c0, (size_t)n));
   PDOS_TRY(tmp.alloc(&err, 1));
-  // row pointer, index and value arrays are padded so that the SpMV's
-  // 16-byte aligned bulk-copy windows stay inside the allocations
-  PDOS_TRY(arena_.alloc(&Ap_, (size_t)n + 16));
-  PDOS_TRY(arena_.alloc(&Ai_, (size_t)nnz + 16));
-  PDOS_TRY(arena_.alloc(&Rp_, (size_t)m + 16));
-  PDOS_TRY(arena_.alloc(&Rj_, (size_t)nnz + 16));
-  PDOS_CUDA_TRY(cudaMemsetAsync(Ap_, 0, sizeof(int32_t) * ((size_t)n + 16), st));
-  PDOS_CUDA_TRY(cudaMemsetAsync(Rp_, 0, sizeof(int32_t) * ((size_t)m + 16), st));
+  // row pointer, index and value arrays are padded by 16 entries
+  PDOS_TRY(arena.alloc(&P.Ap, (size_t)n + 16));
+  PDOS_TRY(arena.alloc(&P.Ai, (size_t)nnz + 16));
+  PDOS_TRY(arena.alloc(&P.Rp, (size_t)m + 16));
+  PDOS_TRY(arena.alloc(&P.Rj, (size_t)nnz + 16));
+  PDOS_CUDA_TRY(cudaMemsetAsync(P.Ap, 0, sizeof(int32_t) * ((size_t)n + 16), st));
+  PDOS_CUDA_TRY(cudaMemsetAsync(P.Rp, 0, sizeof(int32_t) * ((size_t)m + 16), st));
   PDOS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
   if (nnz > 0) {
-    PDOS_CUDA_TRY(cudaMemcpyAsync(Ai64, pr.Ai, sizeof(int64_t) * nnz, cudaMemcpyHostToDevice, st));
-    PDOS_CUDA_TRY(cudaMemcpyAsync(Ax0, pr.Ax, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(Ai64, d.Ai, sizeof(int64_t) * nnz, cudaMemcpyHostToDevice, st));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(Ax0, d.Ax, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
   }
-  PDOS_CUDA_TRY(cudaMemcpyAsync(Ap64, pr.Ap, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
-  PDOS_CUDA_TRY(cudaMemcpyAsync(b0, pr.b, sizeof(double) * m, cudaMemcpyHostToDevice, st));
-  PDOS_CUDA_TRY(cudaMemcpyAsync(c0, pr.c, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(Ap64, d.Ap, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(b0, d.b, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(c0, d.c, sizeof(double) * n, cudaMemcpyHostToDevice, st));
   if (nnz > 0) {
-    narrow_rows_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai64, Ai_, nnz, m, err);
+    narrow_rows_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai64, P.Ai, nnz, m, err);
     finite_check_kernel<<<grid1d(nnz), 256, 0, st>>>(Ax0, nnz, err, 4);
   }
-  narrow_ptr_kernel<<<grid1d(n + 1), 256, 0, st>>>(Ap64, Ap_, n, nnz, err);
+  narrow_ptr_kernel<<<grid1d(n + 1), 256, 0, st>>>(Ap64, P.Ap, n, nnz, err);
   finite_check_kernel<<<grid1d(m), 256, 0, st>>>(b0, m, err, 4);
   finite_check_kernel<<<grid1d(n), 256, 0, st>>>(c0, n, err, 4);
   PDOS_CUDA_TRY(cudaGetLastError());
@@ -276,8 +274,8 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   int32_t *perm = nullptr, *col_of = nullptr;
   PDOS_TRY(tmp.alloc(&perm, (size_t)nnz));
   PDOS_TRY(tmp.alloc(&col_of, (size_t)nnz));
-  PDOS_TRY(device_transpose(m, n, nnz, Ap_, Ai_, Rp_, perm, col_of, tmp, st));
-  if (nnz > 0) gather_col_kernel<<<grid1d(nnz), 256, 0, st>>>(perm, col_of, Rj_, nnz);
+  PDOS_TRY(device_transpose(m, n, nnz, P.Ap, P.Ai, P.Rp, perm, col_of, tmp, st));
+  if (nnz > 0) gather_col_kernel<<<grid1d(nnz), 256, 0, st>>>(perm, col_of, P.Rj, nnz);
 
   // ---- equilibration in double
   double *Aw = nullptr, *bw = nullptr, *cw = nullptr, *xw = nullptr, *yw = nullptr, *sw = nullptr;
@@ -287,68 +285,63 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   PDOS_TRY(tmp.alloc(&xw, (size_t)n));
   PDOS_TRY(tmp.alloc(&yw, (size_t)m));
   PDOS_TRY(tmp.alloc(&sw, (size_t)m));
-  PDOS_TRY(arena_.alloc(&D64_, (size_t)m));
-  PDOS_TRY(arena_.alloc(&E64_, (size_t)n));
+  PDOS_TRY(arena.alloc(&P.D64, (size_t)m));
+  PDOS_TRY(arena.alloc(&P.E64, (size_t)n));
+  double *D64 = P.D64, *E64 = P.E64;
   PDOS_CUDA_TRY(cudaMemsetAsync(xw, 0, sizeof(double) * n, st));
   PDOS_CUDA_TRY(cudaMemsetAsync(yw, 0, sizeof(double) * m, st));
   PDOS_CUDA_TRY(cudaMemsetAsync(sw, 0, sizeof(double) * m, st));
-  if (pr.x0) PDOS_CUDA_TRY(cudaMemcpyAsync(xw, pr.x0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-  if (pr.y0) PDOS_CUDA_TRY(cudaMemcpyAsync(yw, pr.y0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
-  if (pr.s0) PDOS_CUDA_TRY(cudaMemcpyAsync(sw, pr.s0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  if (d.x0) PDOS_CUDA_TRY(cudaMemcpyAsync(xw, d.x0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  if (d.y0) PDOS_CUDA_TRY(cudaMemcpyAsync(yw, d.y0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  if (d.s0) PDOS_CUDA_TRY(cudaMemcpyAsync(sw, d.s0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
 
   // cone row tables (host -> device)
-  const int32_t soc0 = f_ + l_;
   std::vector<int32_t> cone_of_row_h;
-  std::vector<int64_t> cone_off_h(qsize_), cone_len_h(qsize_);
   int32_t *cone_of_row = nullptr;
   int64_t *cone_off = nullptr, *cone_len = nullptr;
-  if (qsize_ > 0) {
+  if (ncones > 0) {
     cone_of_row_h.assign(m, -1);
-    int64_t off = soc0;
-    for (int64_t c = 0; c < qsize_; ++c) {
-      cone_off_h[c] = off;
-      cone_len_h[c] = pr.q[c];
-      for (int64_t i = 0; i < pr.q[c]; ++i) cone_of_row_h[off + i] = (int32_t)c;
-      off += pr.q[c];
-    }
+    for (int64_t c = 0; c < ncones; ++c)
+      for (int64_t i = 0; i < d.soc_len[c]; ++i) cone_of_row_h[d.soc_off[c] + i] = (int32_t)c;
     PDOS_TRY(tmp.alloc(&cone_of_row, (size_t)m));
-    PDOS_TRY(tmp.alloc(&cone_off, (size_t)qsize_));
-    PDOS_TRY(tmp.alloc(&cone_len, (size_t)qsize_));
+    PDOS_TRY(tmp.alloc(&cone_off, (size_t)ncones));
+    PDOS_TRY(tmp.alloc(&cone_len, (size_t)ncones));
     PDOS_CUDA_TRY(cudaMemcpyAsync(cone_of_row, cone_of_row_h.data(), sizeof(int32_t) * m,
                                   cudaMemcpyHostToDevice, st));
-    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_off, cone_off_h.data(), sizeof(int64_t) * qsize_,
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_off, d.soc_off.data(), sizeof(int64_t) * ncones,
                                   cudaMemcpyHostToDevice, st));
-    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_len, cone_len_h.data(), sizeof(int64_t) * qsize_,
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_len, d.soc_len.data(), sizeof(int64_t) * ncones,
                                   cudaMemcpyHostToDevice, st));
   }
 
-  const bool ruiz = pr.normalize && opt.scaling == PDOSGPU_SCALE_RUIZ;
-  if (!pr.normalize) {
-    fill_kernel<<<grid1d(m), 256, 0, st>>>(D64_, m, 1.0);
-    fill_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1.0);
+  const bool ruiz = d.normalize && d.ruiz;
+  if (!d.normalize) {
+    fill_kernel<<<grid1d(m), 256, 0, st>>>(D64, m, 1.0);
+    fill_kernel<<<grid1d(n), 256, 0, st>>>(E64, n, 1.0);
     if (nnz > 0) PDOS_CUDA_TRY(cudaMemcpyAsync(Aw, Ax0, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st));
   } else if (!ruiz) {
     // common.h:69-137
     double *Rx0 = nullptr;
     PDOS_TRY(tmp.alloc(&Rx0, (size_t)nnz));
     if (nnz > 0) gather_kernel<double><<<grid1d(nnz), 256, 0, st>>>(perm, Ax0, Rx0, nnz);
-    row_sumsq_kernel<<<grid1d(m, 128), 128, 0, st>>>(Rp_, Rx0, m, D64_);
-    if (qsize_ > 0) {
+    row_sumsq_kernel<<<grid1d(m, 128), 128, 0, st>>>(P.Rp, Rx0, m, D64);
+    if (ncones > 0) {
       double *mean = nullptr;
-      PDOS_TRY(tmp.alloc(&mean, (size_t)qsize_));
-      cone_mean_kernel<<<grid1d(qsize_, 128), 128, 0, st>>>(D64_, cone_off, cone_len, (int)qsize_, mean);
-      cone_broadcast_kernel<<<grid1d(m - soc0), 256, 0, st>>>(D64_, cone_of_row, mean, soc0, m);
+      PDOS_TRY(tmp.alloc(&mean, (size_t)ncones));
+      cone_mean_kernel<<<grid1d(ncones, 128), 128, 0, st>>>(D64, cone_off, cone_len, (int)ncones, mean);
+      cone_broadcast_kernel<<<grid1d(m), 256, 0, st>>>(D64, cone_of_row, mean, 0, m);
     }
-    clamp_rsqrt_kernel<<<grid1d(m), 256, 0, st>>>(D64_, m);
+    clamp_rsqrt_kernel<<<grid1d(m), 256, 0, st>>>(D64, m);
     if (nnz > 0) {
       PDOS_CUDA_TRY(cudaMemcpyAsync(Aw, Ax0, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st));
-      scale_by_row_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, Ai_, D64_, nnz);
+      scale_by_row_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, P.Ai, D64, nnz);
     }
-    col_sumsq_kernel<<<grid1d(n, 128), 128, 0, st>>>(Ap_, Aw, n, E64_);
-    clamp_rsqrt_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n);
-    if (nnz > 0) scale_by_col_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, col_of, E64_, nnz);
+    col_sumsq_kernel<<<grid1d(n, 128), 128, 0, st>>>(P.Ap, Aw, n, E64);
+    clamp_rsqrt_kernel<<<grid1d(n), 256, 0, st>>>(E64, n);
+    if (nnz > 0) scale_by_col_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, col_of, E64, nnz);
   } else {
     // ruiz_equil_common.h:130-245
+    const int64_t soc0 = d.ruiz_soc0;
     double *cv = nullptr, *cb = nullptr, *rowmax = nullptr, *colmax = nullptr, *sc = nullptr;
     int32_t *ci = nullptr;
     PDOS_TRY(tmp.alloc(&cv, (size_t)nnz));
@@ -357,11 +350,11 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
     PDOS_TRY(tmp.alloc(&rowmax, (size_t)m));
     PDOS_TRY(tmp.alloc(&colmax, (size_t)n));
     PDOS_TRY(tmp.alloc(&sc, 4));
-    if (qsize_ > 0) {
+    if (ncones > 0) {
       int *head = nullptr, *run_excl = nullptr;
       PDOS_TRY(tmp.alloc(&head, (size_t)nnz));
       PDOS_TRY(tmp.alloc(&run_excl, (size_t)nnz + 1));
-      if (nnz > 0) run_heads_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai_, cone_of_row, nnz, head);
+      if (nnz > 0) run_heads_kernel<<<grid1d(nnz), 256, 0, st>>>(P.Ai, cone_of_row, nnz, head);
       PDOS_TRY(device_excl_scan(head, nnz, run_excl, true, tmp, st));
       int nruns = 0;
       PDOS_CUDA_TRY(cudaMemcpyAsync(&nruns, run_excl + nnz, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -370,108 +363,252 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
       PDOS_TRY(tmp.alloc(&runmax, (size_t)nruns));
       PDOS_CUDA_TRY(cudaMemsetAsync(runmax, 0, sizeof(double) * (nruns > 0 ? nruns : 1), st));
       if (nnz > 0) {
-        run_max_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai_, cone_of_row, Ax0, run_excl, head, nnz, runmax);
-        run_apply_kernel<<<grid1d(nnz), 256, 0, st>>>(Ai_, cone_of_row, cone_off, Ax0, run_excl, head,
+        run_max_kernel<<<grid1d(nnz), 256, 0, st>>>(P.Ai, cone_of_row, Ax0, run_excl, head, nnz, runmax);
+        run_apply_kernel<<<grid1d(nnz), 256, 0, st>>>(P.Ai, cone_of_row, cone_off, Ax0, run_excl, head,
                                                       runmax, nnz, cv, ci);
       }
       double *cmax = nullptr;
-      PDOS_TRY(tmp.alloc(&cmax, (size_t)qsize_));
-      PDOS_CUDA_TRY(cudaMemsetAsync(cmax, 0, sizeof(double) * qsize_, st));
+      PDOS_TRY(tmp.alloc(&cmax, (size_t)ncones));
+      PDOS_CUDA_TRY(cudaMemsetAsync(cmax, 0, sizeof(double) * ncones, st));
       cone_absmax_kernel<<<grid1d(m - soc0), 256, 0, st>>>(b0, cone_of_row, soc0, m, cmax);
       cone_collapse_b_kernel<<<grid1d(m), 256, 0, st>>>(b0, cone_of_row, cmax, m, cb);
     } else {
       if (nnz > 0) {
         PDOS_CUDA_TRY(cudaMemcpyAsync(cv, Ax0, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st));
-        PDOS_CUDA_TRY(cudaMemcpyAsync(ci, Ai_, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, st));
+        PDOS_CUDA_TRY(cudaMemcpyAsync(ci, P.Ai, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, st));
       }
       PDOS_CUDA_TRY(cudaMemcpyAsync(cb, b0, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
     }
-    fill_kernel<<<grid1d(m), 256, 0, st>>>(D64_, m, 1.0);
-    fill_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1.0);
+    fill_kernel<<<grid1d(m), 256, 0, st>>>(D64, m, 1.0);
+    fill_kernel<<<grid1d(n), 256, 0, st>>>(E64, n, 1.0);
     PDOS_CUDA_TRY(cudaMemsetAsync(rowmax, 0, sizeof(double) * m, st));
     PDOS_CUDA_TRY(cudaMemsetAsync(colmax, 0, sizeof(double) * n, st));
     const double sc_init[4] = {1.0, 1.0, 0.0, 0.0};
     PDOS_CUDA_TRY(cudaMemcpyAsync(sc, sc_init, sizeof(sc_init), cudaMemcpyHostToDevice, st));
     for (int pass = 0; pass < 3; ++pass) {
-      if (nnz > 0) ruiz_rowmax_kernel<<<grid1d(nnz), 256, 0, st>>>(cv, ci, col_of, E64_, nnz, rowmax);
-      ruiz_lastpi_kernel<<<grid1d(n), 256, 0, st>>>(c0, E64_, n, sc);
+      if (nnz > 0) ruiz_rowmax_kernel<<<grid1d(nnz), 256, 0, st>>>(cv, ci, col_of, E64, nnz, rowmax);
+      ruiz_lastpi_kernel<<<grid1d(n), 256, 0, st>>>(c0, E64, n, sc);
       ruiz_row_finish_kernel<<<grid1d(m), 256, 0, st>>>(cb, sc, m, rowmax);
-      if (qsize_ > 0)
+      if (ncones > 0)
         ruiz_cone_rows_kernel<<<grid1d(m - soc0), 256, 0, st>>>(cone_of_row, cone_off, soc0, m, rowmax);
-      ruiz_update_kernel<<<grid1d(m), 256, 0, st>>>(D64_, rowmax, m);
+      ruiz_update_kernel<<<grid1d(m), 256, 0, st>>>(D64, rowmax, m);
       ruiz_last_kernel<<<1, 32, 0, st>>>(sc, 0);
-      ruiz_colmax_kernel<<<grid1d(n, 128), 128, 0, st>>>(Ap_, cv, ci, D64_, c0, sc, n, colmax);
-      ruiz_lastdelta_kernel<<<grid1d(m), 256, 0, st>>>(cb, D64_, m, sc);
-      ruiz_update_kernel<<<grid1d(n), 256, 0, st>>>(E64_, colmax, n);
+      ruiz_colmax_kernel<<<grid1d(n, 128), 128, 0, st>>>(P.Ap, cv, ci, D64, c0, sc, n, colmax);
+      ruiz_lastdelta_kernel<<<grid1d(m), 256, 0, st>>>(cb, D64, m, sc);
+      ruiz_update_kernel<<<grid1d(n), 256, 0, st>>>(E64, colmax, n);
       ruiz_last_kernel<<<1, 32, 0, st>>>(sc, 1);
     }
-    if (nnz > 0) ruiz_scale_kernel<<<grid1d(nnz), 256, 0, st>>>(Ax0, Ai_, col_of, D64_, E64_, nnz, Aw);
+    if (nnz > 0) ruiz_scale_kernel<<<grid1d(nnz), 256, 0, st>>>(Ax0, P.Ai, col_of, D64, E64, nnz, Aw);
   }
   // c, b and the warm start (common.h:139-161); lambda (common.h:182);
   // x-space ratio (common.h:185-192)
-  if (pr.normalize) {
-    vec_scale_kernel<<<grid1d(n), 256, 0, st>>>(c0, E64_, cw, n, 0);
-    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(b0, D64_, bw, m, 0);
-    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(yw, D64_, yw, m, 1);
-    vec_scale_kernel<<<grid1d(n), 256, 0, st>>>(xw, E64_, xw, n, 1);
-    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(sw, D64_, sw, m, 0);
+  if (d.normalize) {
+    vec_scale_kernel<<<grid1d(n), 256, 0, st>>>(c0, E64, cw, n, 0);
+    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(b0, D64, bw, m, 0);
+    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(yw, D64, yw, m, 1);
+    vec_scale_kernel<<<grid1d(n), 256, 0, st>>>(xw, E64, xw, n, 1);
+    vec_scale_kernel<<<grid1d(m), 256, 0, st>>>(sw, D64, sw, m, 0);
   } else {
     PDOS_CUDA_TRY(cudaMemcpyAsync(cw, c0, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     PDOS_CUDA_TRY(cudaMemcpyAsync(bw, b0, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
   }
   {
-    // lambda = (guard + ||b||) / (guard + ||c||) on the scaled data, summed
-    // sequentially on the host in the reference's order (common.h:182)
+    // lambda = (guard + ||b||) / (guard + ||c||) on the scaled data of each
+    // instance, summed sequentially on the host in the reference's order
+    // (common.h:182)
     std::vector<double> hb(m), hc(n);
     PDOS_CUDA_TRY(cudaMemcpyAsync(hb.data(), bw, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
     PDOS_CUDA_TRY(cudaMemcpyAsync(hc.data(), cw, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-    double sb = 0.0, sc = 0.0;
-    for (int i = 0; i < m; ++i) sb += hb[i] * hb[i];
-    for (int i = 0; i < n; ++i) sc += hc[i] * hc[i];
     const double guard = ruiz ? 1e-6 : 1e-15;
-    lambda_ = (guard + std::sqrt(sb)) / (guard + std::sqrt(sc));
+    P.lambda.assign(ninst, 1.0);
+    for (int64_t k = 0; k < ninst; ++k) {
+      double sb = 0.0, sc = 0.0;
+      for (int64_t i = d.inst_row0[k]; i < d.inst_row0[k + 1]; ++i) sb += hb[i] * hb[i];
+      for (int64_t j = d.inst_col0[k]; j < d.inst_col0[k + 1]; ++j) sc += hc[j] * hc[j];
+      P.lambda[k] = (guard + std::sqrt(sb)) / (guard + std::sqrt(sc));
+    }
   }
-  scal_kernel<<<grid1d(n), 256, 0, st>>>(E64_, n, 1e3, 0);
+  PDOS_TRY(arena.alloc(&P.Epre64, (size_t)n));
+  PDOS_CUDA_TRY(cudaMemcpyAsync(P.Epre64, E64, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(E64, n, 1e3, 0);
   scal_kernel<<<grid1d(n), 256, 0, st>>>(cw, n, 1e3, 0);
   scal_kernel<<<grid1d(n), 256, 0, st>>>(xw, n, 1e3, 1);
   if (nnz > 0) scal_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, nnz, 1e3, 0);
   PDOS_CUDA_TRY(cudaGetLastError());
 
   // ---- working arrays in T
-  PDOS_TRY(arena_.alloc(&Ax_, (size_t)nnz + 16));
-  PDOS_TRY(arena_.alloc(&Rx_, (size_t)nnz + 16));
-  T *bT, *cT, *DT, *ET;
-  PDOS_TRY(arena_.alloc(&bT, (size_t)m));
-  PDOS_TRY(arena_.alloc(&cT, (size_t)n));
-  PDOS_TRY(arena_.alloc(&DT, (size_t)m));
-  PDOS_TRY(arena_.alloc(&ET, (size_t)n));
+  PDOS_TRY(arena.alloc(&P.Ax, (size_t)nnz + 16));
+  PDOS_TRY(arena.alloc(&P.Rx, (size_t)nnz + 16));
+  PDOS_TRY(arena.alloc(&P.b, (size_t)m));
+  PDOS_TRY(arena.alloc(&P.c, (size_t)n));
+  PDOS_TRY(arena.alloc(&P.D, (size_t)m));
+  PDOS_TRY(arena.alloc(&P.E, (size_t)n));
   if (nnz > 0) {
     double *Rxd = nullptr;
     PDOS_TRY(tmp.alloc(&Rxd, (size_t)nnz));
     gather_kernel<double><<<grid1d(nnz), 256, 0, st>>>(perm, Aw, Rxd, nnz);
-    convert_kernel<T><<<grid1d(nnz), 256, 0, st>>>(Aw, Ax_, nnz);
-    convert_kernel<T><<<grid1d(nnz), 256, 0, st>>>(Rxd, Rx_, nnz);
+    convert_kernel<T><<<grid1d(nnz), 256, 0, st>>>(Aw, P.Ax, nnz);
+    convert_kernel<T><<<grid1d(nnz), 256, 0, st>>>(Rxd, P.Rx, nnz);
   }
-  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(bw, bT, m);
-  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(cw, cT, n);
-  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(D64_, DT, m);
-  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(E64_, ET, n);
-  PDOS_TRY(arena_.alloc(&x_init_, (size_t)n));
-  PDOS_TRY(arena_.alloc(&y_init_, (size_t)m));
-  PDOS_TRY(arena_.alloc(&s_init_, (size_t)m));
-  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(xw, x_init_, n);
-  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(yw, y_init_, m);
-  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(sw, s_init_, m);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(bw, P.b, m);
+  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(cw, P.c, n);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(D64, P.D, m);
+  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(E64, P.E, n);
+  PDOS_TRY(arena.alloc(&P.x_init, (size_t)n));
+  PDOS_TRY(arena.alloc(&P.y_init, (size_t)m));
+  PDOS_TRY(arena.alloc(&P.s_init, (size_t)m));
+  convert_kernel<T><<<grid1d(n), 256, 0, st>>>(xw, P.x_init, n);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(yw, P.y_init, m);
+  convert_kernel<T><<<grid1d(m), 256, 0, st>>>(sw, P.s_init, m);
+  PDOS_CUDA_TRY(cudaGetLastError());
+
+  // ---- host copies of both pointer arrays (for the SpMV layouts)
+  P.rp_host.assign((size_t)m + 1, 0);
+  P.ap_host.assign((size_t)n + 1, 0);
+  PDOS_CUDA_TRY(cudaMemcpyAsync(P.rp_host.data(), P.Rp, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, st));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int64_t j = 0; j <= n; ++j) P.ap_host[j] = (int32_t)d.Ap[j];
+  tmp.release();
+  return PDOSGPU_OK;
+}
+
+template int setup_problem<double>(const ProblemDesc &, DeviceArena &, cudaStream_t, DeviceProblem<double> &);
+template int setup_problem<float>(const ProblemDesc &, DeviceArena &, cudaStream_t, DeviceProblem<float> &);
+
+// Cone tables of the grid projection kernels: cones of at most kSmallCone
+// rows go to one warp each, larger ones are cut into kConeChunk-row chunks.
+int build_cone_tables(const std::vector<int64_t> &off_in, const std::vector<int64_t> &len_in,
+                      DeviceArena &arena, cudaStream_t st, ConeTables &ct, int *soc_grid,
+                      int *socbig_grid) {
+  std::vector<int32_t> small_off, small_len, chunk_row0, chunk_row1, chunk_cone, big_head, big_chunk0,
+      big_nchunks;
+  const int64_t ncones = (int64_t)off_in.size();
+  for (int64_t c = 0; c < ncones; ++c) {
+    const int64_t off = off_in[c], q = len_in[c];
+    if (q <= kSmallCone) {
+      small_off.push_back((int32_t)off);
+      small_len.push_back((int32_t)q);
+    } else {
+      const int32_t big = (int32_t)big_head.size();
+      big_head.push_back((int32_t)off);
+      big_chunk0.push_back((int32_t)chunk_row0.size());
+      int32_t nch = 0;
+      for (int64_t r = off; r < off + q; r += kConeChunk) {
+        chunk_row0.push_back((int32_t)r);
+        chunk_row1.push_back((int32_t)std::min<int64_t>(off + q, r + kConeChunk));
+        chunk_cone.push_back(big);
+        ++nch;
+      }
+      big_nchunks.push_back(nch);
+    }
+  }
+  auto up = [&](const std::vector<int32_t> &v, const int32_t **dst) -> int {
+    int32_t *p = nullptr;
+    PDOS_TRY(arena.alloc(&p, v.size() + 1));
+    if (!v.empty())
+      PDOS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, st));
+    *dst = p;
+    return PDOSGPU_OK;
+  };
+  PDOS_TRY(up(small_off, &ct.small_off));
+  PDOS_TRY(up(small_len, &ct.small_len));
+  PDOS_TRY(up(chunk_row0, &ct.chunk_row0));
+  PDOS_TRY(up(chunk_row1, &ct.chunk_row1));
+  PDOS_TRY(up(chunk_cone, &ct.chunk_cone));
+  PDOS_TRY(up(big_head, &ct.big_head));
+  PDOS_TRY(up(big_chunk0, &ct.big_chunk0));
+  PDOS_TRY(up(big_nchunks, &ct.big_nchunks));
+  ct.n_small = (int32_t)small_off.size();
+  ct.n_chunks = (int32_t)chunk_row0.size();
+  PDOS_TRY(arena.alloc(&ct.chunk_sq, chunk_row0.size() + 1));
+  PDOS_TRY(arena.alloc(&ct.big_headval, big_head.size() + 1));
+  const int warps = kBlock / 32;
+  ct.small_blocks = ct.n_small > 0 ? std::min((ct.n_small + warps - 1) / warps, num_sms() * 8) : 0;
+  *soc_grid = ncones > 0 ? ct.small_blocks + ct.n_chunks : 0;
+  *socbig_grid = ct.n_chunks;
+  // the host vectors above go out of scope: wait for their copies
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  return PDOSGPU_OK;
+}
+
+// ============================================================== Engine<T>
+template <typename T>
+int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
+  const double t0 = now_ms();
+  PDOS_TRY(validate_problem(pr));
+  const int64_t nnz64 = pr.Ap[pr.n];
+
+  m_ = (int32_t)pr.m;
+  n_ = (int32_t)pr.n;
+  nnz_ = (int32_t)nnz64;
+  f_ = (int32_t)pr.f;
+  l_ = (int32_t)pr.l;
+  qsize_ = pr.qsize;
+  max_iters_ = pr.max_iters;
+  cg_max_ = pr.cg_max_its;
+  verbose_ = (int)pr.verbose;
+  alpha_ = pr.alpha;
+  eps_ = pr.eps_abs;
+  tol_sq_ = pr.cg_tol * pr.cg_tol;
+
+  ProblemDesc d;
+  d.n = pr.n;
+  d.m = pr.m;
+  d.nnz = nnz64;
+  d.Ax = pr.Ax;
+  d.Ai = pr.Ai;
+  d.Ap = pr.Ap;
+  d.b = pr.b;
+  d.c = pr.c;
+  d.x0 = pr.x0;
+  d.y0 = pr.y0;
+  d.s0 = pr.s0;
+  d.inst_row0 = {0, pr.m};
+  d.inst_col0 = {0, pr.n};
+  d.normalize = pr.normalize ? 1 : 0;
+  d.ruiz = (pr.normalize && opt.scaling == PDOSGPU_SCALE_RUIZ) ? 1 : 0;
+  d.ruiz_soc0 = pr.f + pr.l;
+  {
+    int64_t off = pr.f + pr.l;
+    for (int64_t c = 0; c < pr.qsize; ++c) {
+      d.soc_off.push_back(off);
+      d.soc_len.push_back(pr.q[c]);
+      off += pr.q[c];
+    }
+  }
+
+  PDOS_CUDA_TRY(cudaSetDevice(opt.device));
+  g_num_sms = 0;
+  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  cudaStream_t st = stream_;
+  const int m = m_, n = n_;
+
+  DeviceProblem<T> P;
+  PDOS_TRY(setup_problem<T>(d, arena_, st, P));
+  lambda_ = P.lambda[0];
+  pscale_ = P.pscale[0];
+  dscale_ = P.dscale[0];
+  Ap_ = P.Ap;
+  Ai_ = P.Ai;
+  Rp_ = P.Rp;
+  Rj_ = P.Rj;
+  Ax_ = P.Ax;
+  Rx_ = P.Rx;
+  D64_ = P.D64;
+  E64_ = P.E64;
+  x_init_ = P.x_init;
+  y_init_ = P.y_init;
+  s_init_ = P.s_init;
 
   V_.m = m;
   V_.n = n;
   V_.f = f_;
   V_.l = l_;
-  V_.b = bT;
-  V_.c = cT;
-  V_.D = DT;
-  V_.E = ET;
+  V_.b = P.b;
+  V_.c = P.c;
+  V_.D = P.D;
+  V_.E = P.E;
   PDOS_TRY(arena_.alloc(&V_.x, (size_t)n));
   PDOS_TRY(arena_.alloc(&V_.p, (size_t)n));
   PDOS_TRY(arena_.alloc(&V_.q, (size_t)n));
@@ -489,16 +626,10 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   PDOS_CUDA_TRY(cudaMallocHost(&host_state_, sizeof(DevState)));
   PDOS_CUDA_TRY(cudaMemsetAsync(S_, 0, sizeof(DevState), st));
 
-  // ---- merge-path plans (host, from the two pointer arrays)
-  {
-    std::vector<int32_t> rp(m + 1), ap(n + 1);
-    PDOS_CUDA_TRY(cudaMemcpyAsync(rp.data(), Rp_, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, st));
-    PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-    for (int64_t j = 0; j <= n; ++j) ap[j] = (int32_t)pr.Ap[j];
-    PDOS_TRY(sellA_.build(rp.data(), m, Rj_, Rx_, arena_, st));
-    PDOS_TRY(sellT_.build(ap.data(), n, Ai_, Ax_, arena_, st));
-  }
-  PDOS_TRY(build_cones(pr));
+  // ---- SELL plans of A (rows of A) and A' (columns of A)
+  PDOS_TRY(sellA_.build(P.rp_host.data(), m, Rj_, Rx_, arena_, st));
+  PDOS_TRY(sellT_.build(P.ap_host.data(), n, Ai_, Ax_, arena_, st));
+  PDOS_TRY(build_cone_tables(d.soc_off, d.soc_len, arena_, st, ct_, &soc_grid_, &socbig_grid_));
 
   // ---- grids and reduction scratch (an SpMV kernel uses grid+1 slots)
   grid_upd_ = persistent_grid(cg_update_kernel<T, kBlock>, kBlock, 0, (n + kBlock - 1) / kBlock);
@@ -513,64 +644,10 @@ int Engine<T>::setup(const pdosgpu_problem &pr, const pdosgpu_options &opt) {
   PDOS_CUDA_TRY(cudaMemsetAsync(tickets_, 0, sizeof(unsigned) * 8, st));
 
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-  tmp.release();
   PDOS_TRY(reset());
   PDOS_TRY(build_graph());
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
   setup_ms = now_ms() - t0;
-  return PDOSGPU_OK;
-}
-
-template <typename T>
-int Engine<T>::build_cones(const pdosgpu_problem &pr) {
-  cudaStream_t st = stream_;
-  std::vector<int32_t> small_off, small_len, chunk_row0, chunk_row1, chunk_cone, big_head, big_chunk0,
-      big_nchunks;
-  int64_t off = (int64_t)f_ + l_;
-  for (int64_t c = 0; c < qsize_; ++c) {
-    const int64_t q = pr.q[c];
-    if (q <= kSmallCone) {
-      small_off.push_back((int32_t)off);
-      small_len.push_back((int32_t)q);
-    } else {
-      const int32_t big = (int32_t)big_head.size();
-      big_head.push_back((int32_t)off);
-      big_chunk0.push_back((int32_t)chunk_row0.size());
-      int32_t nch = 0;
-      for (int64_t r = off; r < off + q; r += kConeChunk) {
-        chunk_row0.push_back((int32_t)r);
-        chunk_row1.push_back((int32_t)std::min<int64_t>(off + q, r + kConeChunk));
-        chunk_cone.push_back(big);
-        ++nch;
-      }
-      big_nchunks.push_back(nch);
-    }
-    off += q;
-  }
-  auto up = [&](const std::vector<int32_t> &v, const int32_t **dst) -> int {
-    int32_t *p = nullptr;
-    PDOS_TRY(arena_.alloc(&p, v.size() + 1));
-    if (!v.empty())
-      PDOS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, st));
-    *dst = p;
-    return PDOSGPU_OK;
-  };
-  PDOS_TRY(up(small_off, &ct_.small_off));
-  PDOS_TRY(up(small_len, &ct_.small_len));
-  PDOS_TRY(up(chunk_row0, &ct_.chunk_row0));
-  PDOS_TRY(up(chunk_row1, &ct_.chunk_row1));
-  PDOS_TRY(up(chunk_cone, &ct_.chunk_cone));
-  PDOS_TRY(up(big_head, &ct_.big_head));
-  PDOS_TRY(up(big_chunk0, &ct_.big_chunk0));
-  PDOS_TRY(up(big_nchunks, &ct_.big_nchunks));
-  ct_.n_small = (int32_t)small_off.size();
-  ct_.n_chunks = (int32_t)chunk_row0.size();
-  PDOS_TRY(arena_.alloc(&ct_.chunk_sq, chunk_row0.size() + 1));
-  PDOS_TRY(arena_.alloc(&ct_.big_headval, big_head.size() + 1));
-  const int warps = kBlock / 32;
-  ct_.small_blocks = ct_.n_small > 0 ? std::min((ct_.n_small + warps - 1) / warps, num_sms() * 8) : 0;
-  soc_grid_ = qsize_ > 0 ? ct_.small_blocks + ct_.n_chunks : 0;
-  socbig_grid_ = ct_.n_chunks;
   return PDOSGPU_OK;
 }
 

@@ -265,8 +265,10 @@ __global__ void cone_mean_kernel(const double *D, const int64_t *cone_off, const
 __global__ void cone_broadcast_kernel(double *D, const int32_t *cone_of_row, const double *mean,
                                       int64_t row0, int64_t m) {
   for (int64_t r = row0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
-       r += (int64_t)gridDim.x * blockDim.x)
-    D[r] = mean[cone_of_row[r]];
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = cone_of_row[r];
+    if (c >= 0) D[r] = mean[c];  // rows outside cones keep their own scale
+  }
 }
 
 // v = 1/sqrt(min(max(|v|, 1e-6), 1e6))  (common.h:108-111, :127-130)

@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .abi import Marshalled, read_sol
+from .abi import Cone, Data, Marshalled, Sol, read_sol
 from .problem import DEFAULT_PARAMS, Problem
 
 _PRECISION = {"fp64": _lib.PDOSGPU_FP64, "fp32": _lib.PDOSGPU_FP32}
@@ -33,6 +33,29 @@ def make_options(precision="fp64", scaling="2norm", device=0):
     return opt
 
 
+def _c_problem(prob, keep):
+    """ctypes pdosgpu_problem of a Problem; arrays it points to go to keep."""
+    def f64(a):
+        if a is None:
+            return ctypes.POINTER(ctypes.c_double)()
+        a = np.ascontiguousarray(a, np.float64)
+        keep.append(a)
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    def i64(a):
+        a = np.ascontiguousarray(a, np.int64)
+        keep.append(a)
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+    p = prob.params
+    q = np.asarray(prob.q, np.int64) if len(prob.q) else np.zeros(1, np.int64)
+    return _lib.Problem(
+        prob.n, prob.m, f64(prob.Ax), i64(prob.Ai), i64(prob.Ap), f64(prob.b), f64(prob.c),
+        f64(prob.x0), f64(prob.y0), f64(prob.s0), prob.f, prob.l, len(prob.q), i64(q),
+        int(p["MAX_ITERS"]), int(p["CG_MAX_ITS"]), float(p["EPS_ABS"]), float(p["ALPHA"]),
+        float(p["CG_TOL"]), int(p["VERBOSE"]), int(p["NORMALIZE"]))
+
+
 class Workspace:
     """A problem resident on the GPU (pdosgpu_setup ... pdosgpu_free)."""
 
@@ -40,26 +63,7 @@ class Workspace:
         self.lib = _lib.load()
         self.prob = prob
         self._keep = []
-
-        def f64(a):
-            if a is None:
-                return ctypes.POINTER(ctypes.c_double)()
-            a = np.ascontiguousarray(a, np.float64)
-            self._keep.append(a)
-            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-
-        def i64(a):
-            a = np.ascontiguousarray(a, np.int64)
-            self._keep.append(a)
-            return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
-
-        p = prob.params
-        q = np.asarray(prob.q, np.int64) if len(prob.q) else np.zeros(1, np.int64)
-        self._c_prob = _lib.Problem(
-            prob.n, prob.m, f64(prob.Ax), i64(prob.Ai), i64(prob.Ap), f64(prob.b), f64(prob.c),
-            f64(prob.x0), f64(prob.y0), f64(prob.s0), prob.f, prob.l, len(prob.q), i64(q),
-            int(p["MAX_ITERS"]), int(p["CG_MAX_ITS"]), float(p["EPS_ABS"]), float(p["ALPHA"]),
-            float(p["CG_TOL"]), int(p["VERBOSE"]), int(p["NORMALIZE"]))
+        self._c_prob = _c_problem(prob, self._keep)
         self._opt = make_options(precision, scaling, device)
         self._w = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_setup(ctypes.byref(self._c_prob), ctypes.byref(self._opt),
@@ -120,6 +124,131 @@ class Workspace:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Batch:
+    """Many independent problems solved together (pdosgpu_batch_*): one CTA
+    per instance at a time, convergence masking, per-instance results."""
+
+    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=64):
+        self.lib = _lib.load()
+        self.probs = list(probs)
+        self._keep = []
+        arr = (_lib.Problem * len(self.probs))(*[_c_problem(p, self._keep) for p in self.probs])
+        self._keep.append(arr)
+        self._opt = make_options(precision, "2norm", device)
+        self._b = ctypes.c_void_p()
+        _lib.check(self.lib.pdosgpu_batch_setup(arr, len(self.probs), ctypes.byref(self._opt),
+                                                int(iters_per_launch), ctypes.byref(self._b)),
+                   "pdosgpu_batch_setup", self.lib)
+        self.n_total = sum(p.n for p in self.probs)
+        self.m_total = sum(p.m for p in self.probs)
+
+    def solve(self):
+        _lib.check(self.lib.pdosgpu_batch_solve(self._b), "pdosgpu_batch_solve", self.lib)
+        return self
+
+    def launch(self, launches):
+        _lib.check(self.lib.pdosgpu_batch_launch(self._b, int(launches)), "pdosgpu_batch_launch",
+                   self.lib)
+        return self
+
+    def reset(self):
+        _lib.check(self.lib.pdosgpu_batch_reset(self._b), "pdosgpu_batch_reset", self.lib)
+        return self
+
+    def warm_start(self, x0=None, y0=None, s0=None):
+        """Starting iterates from device pointers (ints) of stacked float64
+        arrays in the caller's units; None keeps the current one."""
+        _lib.check(self.lib.pdosgpu_batch_warm_start(self._b, x0, y0, s0),
+                   "pdosgpu_batch_warm_start", self.lib)
+        return self
+
+    def done(self):
+        return int(self.lib.pdosgpu_batch_done(self._b))
+
+    def tune(self, iters=8):
+        blocks = (ctypes.c_int * 4)()
+        _lib.check(self.lib.pdosgpu_batch_tune(self._b, int(iters), blocks), "pdosgpu_batch_tune",
+                   self.lib)
+        return list(blocks)
+
+    def set_blocks(self, blocks):
+        arr = (ctypes.c_int * 4)(*blocks)
+        _lib.check(self.lib.pdosgpu_batch_set_blocks(self._b, arr), "pdosgpu_batch_set_blocks",
+                   self.lib)
+        return self
+
+    @property
+    def stream(self):
+        return self.lib.pdosgpu_batch_stream(self._b)
+
+    def fetch_all(self):
+        """Stacked x, s, y and a list of per-instance info dicts."""
+        cnt = len(self.probs)
+        x, s, y = np.zeros(self.n_total), np.zeros(self.m_total), np.zeros(self.m_total)
+        infos = (_lib.Info * cnt)()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _lib.check(self.lib.pdosgpu_batch_fetch(self._b, 0, cnt, x.ctypes.data_as(dp),
+                                                s.ctypes.data_as(dp), y.ctypes.data_as(dp),
+                                                infos), "pdosgpu_batch_fetch", self.lib)
+        out = []
+        for inf in infos:
+            d = inf.as_dict()
+            d["lambda"] = d.pop("lambda_")
+            out.append(d)
+        return x, s, y, out
+
+    def fetch(self):
+        """One result dict per instance, as Workspace.fetch returns."""
+        x, s, y, infos = self.fetch_all()
+        res, c0, r0 = [], 0, 0
+        for p, d in zip(self.probs, infos):
+            res.append({"x": x[c0:c0 + p.n].copy(), "s": s[r0:r0 + p.m].copy(),
+                        "y": y[r0:r0 + p.m].copy(),
+                        "status": "Solved" if d["solved"] else "Indeterminate",
+                        "iters": d["admm_iters"], "cg_iters": d["cg_iters"], "info": d})
+            c0 += p.n
+            r0 += p.m
+        return res
+
+    def close(self):
+        if self._b:
+            self.lib.pdosgpu_batch_free(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def pdos_batch_call(probs, precision=None, libname="libpdosindir.so"):
+    """Solve a list of problems through the reference-style ``pdos_batch()``."""
+    lib = _lib.load(libname)
+    mars = [Marshalled(p) for p in probs]
+    cnt = len(probs)
+    dps = (ctypes.POINTER(Data) * cnt)(*[ctypes.pointer(m.data) for m in mars])
+    kps = (ctypes.POINTER(Cone) * cnt)(*[ctypes.pointer(m.cone) for m in mars])
+    sols = (ctypes.POINTER(Sol) * cnt)()
+    infos = (_lib.Info * cnt)()
+    opt = make_options(precision or "fp64")
+    rc = lib.pdos_batch(dps, kps, cnt, ctypes.byref(opt), sols, infos)
+    _lib.check(rc, "pdos_batch", lib)
+    out = []
+    for i, p in enumerate(probs):
+        x, s, y, status = read_sol(sols[i], p.n, p.m)
+        lib.freeSol(ctypes.byref(sols[i]))
+        out.append({"x": x, "s": s, "y": y, "status": status, "iters": infos[i].admm_iters,
+                    "cg_iters": infos[i].cg_iters})
+    return out
 
 
 def solve_problem(prob, precision="fp64", scaling="2norm"):

@@ -1,0 +1,195 @@
+"""Batched solving of many independent problems (pdosgpu_batch_*, pdos_batch).
+
+Every instance of a batch must give what the reference's own solver gives for
+that instance alone, at the bar of the single-instance parity tests: the
+golden cases run as two batches (one per NORMALIZE value) and each result is
+held to its golden with check_parity.  Uneven portfolio instances that reach
+every size class, the CTA-wide cone path (cones above 1024 rows) and split
+rows (above 256 nonzeros) are compared with the single-instance GPU solver
+and with the oracle.  The rest pins the batch mechanics: results do not
+depend on how many iterations a launch runs, repeated solves are
+bit-identical, device warm starts equal set-up warm starts, and the C entry
+point pdos_batch returns what the Python wrapper returns."""
+import numpy as np
+import pytest
+
+from golden_util import check_parity, load_case, rel, solve_cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+def _golden_groups():
+    groups = {0: [], 1: []}
+    for name in solve_cases():
+        prob, ref = load_case(name)
+        if ref["variant"] == "ruiz":
+            continue  # Ruiz scaling is single-instance only
+        groups[int(prob.params["NORMALIZE"])].append((name, prob, ref))
+    return groups
+
+
+@pytest.mark.parametrize("normalize", [0, 1])
+def test_batch_of_goldens_matches_reference(built_lib, torch_cuda, normalize):
+    from pdos_gb300.solver import Batch
+    cases = _golden_groups()[normalize]
+    assert len(cases) >= 5
+    with Batch([p for _, p, _ in cases]) as b:
+        outs = b.solve().fetch()
+    for (name, prob, ref), out in zip(cases, outs):
+        try:
+            check_parity(prob, ref, out, vec_tol=1e-4 if ref["iters"] >= 1000 else 1e-6)
+        except AssertionError as e:
+            raise AssertionError(f"{name}: {e}") from e
+
+
+def _uneven_portfolios(eps=1e-4):
+    from pdos_gb300 import generators as g
+    shapes = [(20, 2, 0.5), (150, 15, 0.2), (400, 40, 0.2), (900, 90, 0.2), (1500, 30, 0.2),
+              (60, 6, 0.5), (3700, 370, 0.2)]
+    probs = []
+    for i, (n, k, dens) in enumerate(shapes):
+        probs.append(g.portfolio(n, k, dens, seed=40 + i,
+                                 params=dict(EPS_ABS=eps, VERBOSE=0, MAX_ITERS=3000)))
+    # a random-cone split (many small SOCs) and different per-instance parameters
+    probs.append(g.portfolio(300, 30, 0.2, seed=77, random_soc_split=True,
+                             params=dict(EPS_ABS=eps, VERBOSE=0, MAX_ITERS=3000, ALPHA=1.6,
+                                         CG_MAX_ITS=12)))
+    return probs
+
+
+def test_uneven_batch_matches_single_instance_solves(built_lib, torch_cuda):
+    from pdos_gb300.solver import Batch, solve_problem
+    probs = _uneven_portfolios()
+    nnz = [len(p.Ax) for p in probs]
+    assert min(nnz) <= 4096 and max(nnz) > 262144  # all four size classes
+    assert any(max(p.q) > 1024 for p in probs)    # CTA-wide cone path
+    with Batch(probs) as b:
+        outs = b.solve().fetch()
+    for i, (p, out) in enumerate(zip(probs, outs)):
+        single = solve_problem(p)
+        assert out["status"] == single["status"] == "Solved", i
+        assert abs(out["iters"] - single["iters"]) <= max(3, 0.02 * single["iters"]), \
+            (i, out["iters"], single["iters"])
+        o_b, o_s = float(p.c @ out["x"]), float(p.c @ single["x"])
+        assert abs(o_b - o_s) <= 1e-5 * max(1.0, abs(o_s)), (i, o_b, o_s)
+        for k in ("x", "s", "y"):
+            assert rel(out[k], single[k]) <= 1e-4, (i, k, rel(out[k], single[k]))
+
+
+def test_uneven_batch_matches_oracle(built_lib, torch_cuda, port):
+    from pdos_gb300.solver import Batch
+    probs = [p for p in _uneven_portfolios() if len(p.Ax) < 100000]
+    with Batch(probs) as b:
+        outs = b.solve().fetch()
+    for i, (p, out) in enumerate(zip(probs, outs)):
+        ref = port.port_solve(p)
+        assert out["status"] == ref["status"], i
+        o_r = float(p.c @ ref["x"])
+        assert abs(float(p.c @ out["x"]) - o_r) <= 1e-3 * max(1.0, abs(o_r)), i
+
+
+def test_fp32_batch_reaches_fp64_oracle(built_lib, torch_cuda, port):
+    from pdos_gb300.solver import Batch
+    probs = [p for p in _uneven_portfolios() if len(p.Ax) < 20000]
+    with Batch(probs, precision="fp32") as b:
+        outs = b.solve().fetch()
+    for i, (p, out) in enumerate(zip(probs, outs)):
+        hi = port.port_solve(p.with_params(EPS_ABS=1e-7, MAX_ITERS=20000, CG_MAX_ITS=60,
+                                           CG_TOL=1e-12))
+        assert out["status"] == "Solved", i
+        o_hi = float(p.c @ hi["x"])
+        assert abs(float(p.c @ out["x"]) - o_hi) <= 1e-3 * max(1.0, abs(o_hi)), i
+
+
+def test_results_do_not_depend_on_iterations_per_launch(built_lib, torch_cuda):
+    from pdos_gb300.solver import Batch
+    probs = _uneven_portfolios()[:5]
+    with Batch(probs, iters_per_launch=3) as a, Batch(probs, iters_per_launch=500) as b:
+        ra, rb = a.solve().fetch(), b.solve().fetch()
+        again = a.reset().solve().fetch()
+    for x, y, z in zip(ra, rb, again):
+        assert x["iters"] == y["iters"] == z["iters"]
+        assert x["cg_iters"] == y["cg_iters"] == z["cg_iters"]
+        for k in ("x", "s", "y"):
+            assert np.array_equal(x[k], y[k]) and np.array_equal(x[k], z[k])
+
+
+def test_device_warm_start_equals_setup_warm_start(built_lib, torch_cuda):
+    from pdos_gb300.solver import Batch
+    torch = torch_cuda
+    probs = _uneven_portfolios()[:4]
+    with Batch(probs) as b:
+        b.solve()
+        x, s, y, infos = b.fetch_all()
+        cold_iters = [d["admm_iters"] for d in infos]
+        # restart from the solution: every instance stops at once
+        dx = torch.as_tensor(x, device="cuda")
+        dy = torch.as_tensor(y, device="cuda")
+        ds = torch.as_tensor(s, device="cuda")
+        b.warm_start(dx.data_ptr(), dy.data_ptr(), ds.data_ptr()).solve()
+        warm = b.fetch()
+    assert all(w["iters"] <= 1 for w in warm), [w["iters"] for w in warm]
+    assert max(cold_iters) > 20
+    # the same start given at set-up time gives the same bits
+    starts, c0, r0 = [], 0, 0
+    for p in probs:
+        starts.append(p.with_warm_start(x[c0:c0 + p.n], y[r0:r0 + p.m], s[r0:r0 + p.m]))
+        c0 += p.n
+        r0 += p.m
+    with Batch(starts) as b2:
+        warm2 = b2.solve().fetch()
+    for u, v in zip(warm, warm2):
+        assert u["iters"] == v["iters"]
+        for k in ("x", "s", "y"):
+            assert np.array_equal(u[k], v[k])
+
+
+def test_pdos_batch_abi_equals_wrapper(built_lib, torch_cuda):
+    from pdos_gb300.solver import Batch, pdos_batch_call
+    probs = _uneven_portfolios()[:3]
+    abi = pdos_batch_call(probs)
+    with Batch(probs) as b:
+        wr = b.solve().fetch()
+    for u, v in zip(abi, wr):
+        assert u["status"] == v["status"] and u["iters"] == v["iters"]
+        for k in ("x", "s", "y"):
+            assert np.array_equal(u[k], v[k])
+
+
+def test_autotuner_choice_is_reproducible(built_lib, torch_cuda):
+    from pdos_gb300.solver import Batch
+    probs = _uneven_portfolios()[:6]
+    with Batch(probs) as b:
+        blocks = b.tune(iters=4)
+        assert all(v in (128, 256, 512) for v in blocks)
+        tuned = b.solve().fetch()
+    with Batch(probs) as b2:
+        fixed = b2.set_blocks(blocks).solve().fetch()
+    for u, v in zip(tuned, fixed):
+        assert u["iters"] == v["iters"]
+        for k in ("x", "s", "y"):
+            assert np.array_equal(u[k], v[k])
+
+
+def test_batch_rejects_what_it_cannot_run(built_lib, torch_cuda):
+    from pdos_gb300 import generators as g
+    from pdos_gb300.solver import Batch
+    a = g.portfolio(50, 5, 0.5, seed=1, params=dict(NORMALIZE=0, VERBOSE=0))
+    b = g.portfolio(50, 5, 0.5, seed=2, params=dict(NORMALIZE=1, VERBOSE=0))
+    with pytest.raises(RuntimeError, match="NORMALIZE"):
+        Batch([a, b])
+    big = g.random_feasible(m=40000, n=2, nnz_per_col=3, zero_frac=1.0, nonneg_frac=0.0, seed=3,
+                            params=dict(VERBOSE=0))
+    with pytest.raises(RuntimeError, match="shared memory"):
+        Batch([a, big])
+    # the GPU stays usable
+    with Batch([a]) as ok:
+        assert ok.solve().fetch()[0]["status"] in ("Solved", "Indeterminate")
