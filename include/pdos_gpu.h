@@ -156,6 +156,12 @@ int64_t pdosgpu_batch_done(pdosgpu_batch *b);
  * (128, 256, 512), keeps the fastest, resets the batch; blocks (may be
  * NULL) receives the choice for the four classes. */
 int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks);
+/* Roofline timing: the two CG products (u = A p, t = p + A'u) of every
+ * instance, `reps` times, with nothing else; *ms = device time of the
+ * launches, *bytes (may be NULL) = their algorithmic bytes (values and
+ * indices of A and A', both pointer arrays, the vector gathered and the
+ * vector written, per product).  Leaves the iterate untouched. */
+int pdosgpu_batch_time_products(pdosgpu_batch *b, int reps, double *ms, double *bytes);
 /* Set the CTA size of the four size classes explicitly. */
 int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks);
 /* Number of instances and stacked sizes (any may be NULL). */

@@ -87,6 +87,7 @@ SIGNATURES = {
     "pdosgpu_batch_done": (c_int64, [c_void_p]),
     "pdosgpu_batch_tune": (c_int, [c_void_p, c_int, POINTER(c_int)]),
     "pdosgpu_batch_set_blocks": (c_int, [c_void_p, POINTER(c_int)]),
+    "pdosgpu_batch_time_products": (c_int, [c_void_p, c_int, POINTER(c_double), POINTER(c_double)]),
     "pdosgpu_batch_sizes": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64),
                                     POINTER(c_int64), POINTER(c_int64)]),
     "pdosgpu_batch_stream": (c_void_p, [c_void_p]),

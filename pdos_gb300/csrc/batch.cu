@@ -128,9 +128,63 @@ __device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
   __syncthreads();
 }
 
+// Streaming loads of four consecutive matrix entries (16-byte aligned):
+// read-only for the kernel's lifetime and not kept in L1, which holds the
+// instance's vectors instead.
+struct Idx4 {
+  int x, y, z, w;
+};
+__device__ __forceinline__ Idx4 ld_stream4(const int32_t *p) {
+  Idx4 r;
+  asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+template <typename T>
+struct Val4 {
+  T x, y, z, w;
+};
+__device__ __forceinline__ Val4<float> ld_stream4(const float *p) {
+  Val4<float> r;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(p));
+  return r;
+}
+__device__ __forceinline__ Val4<double> ld_stream4(const double *p) {
+  Val4<double> r;
+  asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];"
+               : "=d"(r.x), "=d"(r.y)
+               : "l"(p));
+  asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];"
+               : "=d"(r.z), "=d"(r.w)
+               : "l"(p + 2));
+  return r;
+}
+
+// Four consecutive entries of one row into the NV running sums, in order.
+template <typename T, int NV>
+__device__ __forceinline__ void fma4(const Idx4 &j, const Val4<T> &v, const T *src0, const T *src1,
+                                     T &a0, T &a1) {
+  a0 = fma(v.x, src0[j.x], a0);
+  a0 = fma(v.y, src0[j.y], a0);
+  a0 = fma(v.z, src0[j.z], a0);
+  a0 = fma(v.w, src0[j.w], a0);
+  if (NV == 2) {
+    a1 = fma(v.x, src1[j.x], a1);
+    a1 = fma(v.y, src1[j.y], a1);
+    a1 = fma(v.z, src1[j.z], a1);
+    a1 = fma(v.w, src1[j.w], a1);
+  }
+}
+
 // y-side of one product over one side of an instance: NV source vectors
-// (in shared or global memory), rows handed to epi(row, sum0, sum1).  Split
-// rows leave piece partials in pbuf and are finished after a barrier.
+// (in shared or global memory), rows handed to epi(row, sum0, sum1).
+// Pieces are 4-aligned runs of one row (lane l takes entries 4l..4l+3 of
+// every 128); slices of width >= 4 are stored four columns at a time per
+// lane ([c/4][lane][c%4]), narrower ones one column at a time ([c][lane]).
+// Split rows leave piece partials in pbuf and are finished after a barrier.
 template <typename T, int BLOCK, int NV, class Epi>
 __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, const T *src0,
                                             const T *src1, T *pbuf, Epi &&epi) {
@@ -140,14 +194,15 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     const int64_t pk = sd.piece0 + k;
     const int32_t prow = H.piece_row[pk];
     const int64_t beg = H.piece_beg[pk];
-    const int len = H.piece_len[pk];
+    const int len = H.piece_len[pk];  // a multiple of 4
     T a0 = T(0), a1 = T(0);
-#pragma unroll 4
-    for (int e = lane; e < len; e += 32) {
-      const int j = H.idx[beg + e];
-      const T v = H.val[beg + e];
-      a0 = fma(v, src0[j], a0);
-      if (NV == 2) a1 = fma(v, src1[j], a1);
+    const int32_t *ip = H.idx + beg;
+    const T *vp = H.val + beg;
+#pragma unroll 2
+    for (int e = 4 * lane; e < len; e += 128) {
+      const Idx4 j = ld_stream4(ip + e);
+      const Val4<T> v = ld_stream4(vp + e);
+      fma4<T, NV>(j, v, src0, src1, a0, a1);
     }
     a0 = warp_sum_t(a0);
     if (NV == 2) a1 = warp_sum_t(a1);
@@ -165,14 +220,24 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     const int64_t off = H.slice_beg[sk];
     const int width = H.slice_w[sk];
     T a0 = T(0), a1 = T(0);
-    const int32_t *ip = H.idx + off + lane;
-    const T *vp = H.val + off + lane;
-#pragma unroll 4
-    for (int c = 0; c < width; ++c) {
-      const int j = ip[c * 32];
-      const T v = vp[c * 32];
-      a0 = fma(v, src0[j], a0);
-      if (NV == 2) a1 = fma(v, src1[j], a1);
+    if (width < 0) {  // four columns per lane and load
+      const int32_t *ip = H.idx + off + 4 * lane;
+      const T *vp = H.val + off + 4 * lane;
+#pragma unroll 2
+      for (int c4 = 0; c4 < -width; c4 += 4) {
+        const Idx4 j = ld_stream4(ip + 32 * c4);
+        const Val4<T> v = ld_stream4(vp + 32 * c4);
+        fma4<T, NV>(j, v, src0, src1, a0, a1);
+      }
+    } else {
+      const int32_t *ip = H.idx + off + lane;
+      const T *vp = H.val + off + lane;
+      for (int c = 0; c < width; ++c) {
+        const int j = ip[c * 32];
+        const T v = vp[c * 32];
+        a0 = fma(v, src0[j], a0);
+        if (NV == 2) a1 = fma(v, src1[j], a1);
+      }
     }
     if (!((H.slice_skip[sk] >> lane) & 1u)) epi(s * 32 + lane, a0, a1);
   }
@@ -205,10 +270,17 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
                                T *g2, T *tt, T *pbuf, double *scratch) {
   const int tid = threadIdx.x;
   const int m = I.m, n = I.n, f = I.f, l = I.l;
-  T *x = B.x + I.col0, *q = B.q + I.col0;
-  T *s = B.s + I.row0, *y = B.y + I.row0, *st = B.st + I.row0, *u = B.u + I.row0,
-    *ax = B.ax + I.row0;
-  const T *b = B.b + I.row0, *D = B.D + I.row0, *c = B.c + I.col0, *E = B.E + I.col0;
+  T *__restrict__ x = B.x + I.col0;
+  T *__restrict__ q = B.q + I.col0;
+  T *__restrict__ s = B.s + I.row0;
+  T *__restrict__ y = B.y + I.row0;
+  T *__restrict__ st = B.st + I.row0;
+  T *__restrict__ u = B.u + I.row0;
+  T *__restrict__ ax = B.ax + I.row0;
+  const T *__restrict__ b = B.b + I.row0;
+  const T *__restrict__ D = B.D + I.row0;
+  const T *__restrict__ c = B.c + I.col0;
+  const T *__restrict__ E = B.E + I.col0;
   const T lam = (T)I.lambda;
   const T alpha = (T)I.alpha, oma = (T)(1.0 - I.alpha);
 
@@ -299,6 +371,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       const double step = qsold / pt[0];
       const T stp = (T)step, nstp = (T)(-step);
       double qs[1] = {0.0};
+#pragma unroll 4
       for (int j = tid; j < n; j += BLOCK) {
         x[j] = x[j] + stp * g1[j];
         const T qj = q[j] + nstp * tt[j];
@@ -318,6 +391,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       }
       if (active) {
         const T beta = (T)ratio;
+#pragma unroll 4
         for (int j = tid; j < n; j += BLOCK) g1[j] = beta * g1[j] + q[j];
         __syncthreads();
       }
@@ -397,7 +471,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
 }
 
 template <typename T, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 1) batch_admm_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double scratch[3 * (BLOCK / 32)];
   __shared__ Inst s_inst;
@@ -419,6 +493,44 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_admm_kernel(Dev<T> B, int cls,
           reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
     __syncthreads();
     solve_instance<T, BLOCK>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch);
+  }
+}
+
+// The two CG products alone (u = A p, t = p + A'u), `reps` times for every
+// instance of a class, for the roofline of the batch's SpMV: no reductions,
+// no stop test, the iterate untouched (p is the current x).
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev<T> B, int cls, Smem sm,
+                                                                              int reps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Inst s_inst;
+  __shared__ int s_k;
+  T *g1 = reinterpret_cast<T *>(smem_raw);
+  T *g2 = g1 + sm.g1;
+  T *tt = g2 + sm.g2;
+  T *pbuf = tt + sm.tt;
+  const int begin = B.class_begin[cls], count = B.class_begin[cls + 1] - begin;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_k = atomicAdd(&B.queue[cls], 1);
+    __syncthreads();
+    const int k = s_k;
+    if (k >= count) break;
+    const int id = B.order[begin + k];
+    if (threadIdx.x < (int)(sizeof(Inst) / 4))
+      reinterpret_cast<int32_t *>(&s_inst)[threadIdx.x] =
+          reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
+    __syncthreads();
+    const Inst &I = s_inst;
+    const T *x = B.x + I.col0;
+    for (int j = threadIdx.x; j < I.n; j += BLOCK) g1[j] = x[j];
+    __syncthreads();
+    for (int r = 0; r < reps; ++r) {
+      hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int row, T a, T) { g2[row] = a; });
+      __syncthreads();
+      hyb_product<T, BLOCK, 1>(B.At, I.At, g2, g2, pbuf, [&](int j, T a, T) { tt[j] = g1[j] + a; });
+      __syncthreads();
+    }
   }
 }
 
@@ -501,21 +613,28 @@ struct HybBuild {
         }
         width = std::max(width, len);
       }
+      const bool vec = width >= 4;
+      if (vec) {
+        width = (width + 3) & ~3;
+        pad4();
+      }
       slice_beg.push_back((int64_t)idx.size());
-      slice_w.push_back(width);
-      for (int cidx = 0; cidx < width; ++cidx) {
+      slice_w.push_back(vec ? -width : width);
+      for (int cidx = 0; cidx < width; cidx += vec ? 4 : 1) {
         for (int lane = 0; lane < 32; ++lane) {
-          const int64_t r = s0 + lane;
-          int32_t j = 0, p = -1;
-          if (!((skip >> lane) & 1u)) {
-            const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
-            if (cidx < len) {
-              p = (int32_t)(a + cidx);
-              j = (int32_t)(gidx[a + cidx] - c0);
+          for (int t = 0; t < (vec ? 4 : 1); ++t) {
+            const int64_t r = s0 + lane;
+            int32_t j = 0, p = -1;
+            if (!((skip >> lane) & 1u)) {
+              const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
+              if (cidx + t < len) {
+                p = (int32_t)(a + cidx + t);
+                j = (int32_t)(gidx[a + cidx + t] - c0);
+              }
             }
+            idx.push_back(j);
+            src.push_back(p);
           }
-          idx.push_back(j);
-          src.push_back(p);
         }
       }
       slice_skip.push_back(skip);
@@ -533,22 +652,28 @@ struct HybBuild {
       }
       for (int64_t k = 0; k < np; ++k) {  // nearly equal pieces
         const int64_t e0 = a + len * k / np, e1 = a + len * (k + 1) / np;
+        pad4();
         piece_row.push_back(np > 1 ? ~(int32_t)r : (int32_t)r);
         piece_beg.push_back((int64_t)idx.size());
-        piece_len.push_back((int32_t)(e1 - e0));
         for (int64_t e = e0; e < e1; ++e) {
           idx.push_back((int32_t)(gidx[e] - c0));
           src.push_back((int32_t)e);
         }
+        pad4();
+        piece_len.push_back((int32_t)((int64_t)idx.size() - piece_beg.back()));
         ++sd.npieces;
       }
     }
-    // pad to a multiple of 4 elements so that the next instance starts aligned
+    pad4();
+    return sd;
+  }
+
+  // zero entries up to the next multiple of 4 (16-byte alignment)
+  void pad4() {
     while (idx.size() % 4) {
       idx.push_back(0);
       src.push_back(-1);
     }
-    return sd;
   }
 };
 
@@ -612,6 +737,7 @@ class BatchBase {
   virtual int fetch(int64_t first, int64_t count, double *x, double *s, double *y,
                     pdosgpu_info *info) = 0;
   virtual int tune(int iters, int *blocks_out) = 0;
+  virtual int time_products(int reps, double *ms, double *bytes) = 0;
   virtual int set_blocks(const int *blocks) = 0;
   virtual void *stream() = 0;
   virtual int64_t done_count() = 0;
@@ -644,6 +770,7 @@ class BatchEngine : public BatchBase {
   int warm_start(const double *x0, const double *y0, const double *s0) override;
   int fetch(int64_t first, int64_t cnt, double *x, double *s, double *y, pdosgpu_info *info) override;
   int tune(int iters, int *blocks_out) override;
+  int time_products(int reps, double *ms, double *bytes) override;
   int set_blocks(const int *blocks) override;
   void *stream() override { return stream_; }
   int64_t done_count() override;
@@ -668,6 +795,7 @@ class BatchEngine : public BatchBase {
   int32_t *queue_ = nullptr, *ndone_ = nullptr;
   int32_t *host_done_ = nullptr;
   std::vector<Inst> inst_h_;
+  std::vector<int64_t> nnz_h_;
   std::vector<int32_t> class_begin_h_;
   Smem smem_[kClasses]{};
   int block_[kClasses]{};
@@ -813,6 +941,7 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     I.max_iters = p.max_iters;
     I.cg_max = p.cg_max_its;
     const int64_t nz = p.Ap[p.n];
+    nnz_h_.push_back(nz);
     int cls = 0;
     while (cls < kClasses - 1 && nz > kClassNnz[cls]) ++cls;
     I.cls = cls;
@@ -1176,6 +1305,63 @@ int BatchEngine<T>::tune(int iters, int *blocks_out) {
   return build_graph(iter_cap_, &exec_[0]);
 }
 
+// The CG products of every instance `reps` times (batch_products_kernel),
+// class after class on the batch stream; bytes = the algorithmic bytes of
+// those products (values and indices of A and A', both pointer arrays, the
+// vector gathered from and the vector written, per product).
+template <typename T>
+int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
+  if (reps <= 0 || !ms) return fail(PDOSGPU_EINVAL, "reps must be positive");
+  cudaStream_t st = stream_;
+  double b = 0.0;
+  for (int64_t i = 0; i < count; ++i) {
+    const double sv = sizeof(T), m = inst_h_[i].m, n = inst_h_[i].n, nz = (double)nnz_h_[i];
+    b += nz * (sv + 4) + (m + 1) * 4 + n * sv + m * sv;  // u = A p
+    b += nz * (sv + 4) + (n + 1) * 4 + m * sv + n * sv;  // t = p + A'u
+  }
+  auto go = [&](int cls, int block, auto kernel) -> int {
+    const size_t sm_bytes = smem_[cls].bytes(sizeof(T));
+    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bytes));
+    int per_sm = 0;
+    PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, sm_bytes));
+    if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "product kernel does not fit on an SM");
+    const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
+    const int grid = std::max(1, std::min(members, per_sm * num_sms()));
+    kernel<<<grid, block, sm_bytes, st>>>(dev_, cls, smem_[cls], reps);
+    PDOS_CUDA_TRY(cudaGetLastError());
+    return PDOSGPU_OK;
+  };
+  auto all = [&]() -> int {
+    PDOS_CUDA_TRY(cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st));
+    for (int k = 0; k < kClasses; ++k) {
+      if (class_begin_h_[k + 1] == class_begin_h_[k]) continue;
+      switch (block_[k]) {
+        case 128: PDOS_TRY(go(k, 128, batch_products_kernel<T, 128>)); break;
+        case 256: PDOS_TRY(go(k, 256, batch_products_kernel<T, 256>)); break;
+        default: PDOS_TRY(go(k, 512, batch_products_kernel<T, 512>)); break;
+      }
+    }
+    launches += kClasses;
+    return PDOSGPU_OK;
+  };
+  cudaEvent_t e0, e1;
+  PDOS_CUDA_TRY(cudaEventCreate(&e0));
+  PDOS_CUDA_TRY(cudaEventCreate(&e1));
+  int rc = all();  // warm-up
+  if (rc == PDOSGPU_OK && cudaEventRecord(e0, st) != cudaSuccess) rc = fail(PDOSGPU_ECUDA, "event");
+  if (rc == PDOSGPU_OK) rc = all();
+  if (rc == PDOSGPU_OK && cudaEventRecord(e1, st) != cudaSuccess) rc = fail(PDOSGPU_ECUDA, "event");
+  float t = 0.f;
+  if (rc == PDOSGPU_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(PDOSGPU_ECUDA, "product kernels failed");
+  if (rc == PDOSGPU_OK) cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  PDOS_TRY(rc);
+  *ms = t;
+  if (bytes) *bytes = b * reps;
+  return PDOSGPU_OK;
+}
+
 }  // namespace batch
 }  // namespace pdosgpu
 
@@ -1256,6 +1442,11 @@ int64_t pdosgpu_batch_done(pdosgpu_batch *b) {
 int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks) {
   if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
   return b->engine->tune(iters, blocks);
+}
+
+int pdosgpu_batch_time_products(pdosgpu_batch *b, int reps, double *ms, double *bytes) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->time_products(reps, ms, bytes);
 }
 
 int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks) {

@@ -173,6 +173,14 @@ class Batch:
                    self.lib)
         return list(blocks)
 
+    def time_products(self, reps=4):
+        """(ms, algorithmic bytes) of `reps` CG product pairs of every instance."""
+        ms, nb = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self.lib.pdosgpu_batch_time_products(self._b, int(reps), ctypes.byref(ms),
+                                                        ctypes.byref(nb)),
+                   "pdosgpu_batch_time_products", self.lib)
+        return ms.value, nb.value
+
     def set_blocks(self, blocks):
         arr = (ctypes.c_int * 4)(*blocks)
         _lib.check(self.lib.pdosgpu_batch_set_blocks(self._b, arr), "pdosgpu_batch_set_blocks",

@@ -62,6 +62,11 @@ def check_parity(prob, ref, out, vec_tol=VEC_TOL, iter_slack=0.01):
     obj = float(prob.c @ out["x"])
     obj_tol = max(1e-3 * max(1.0, abs(obj_ref)), 5.0 * (ref["sens_obj_hi"] - ref["sens_obj_lo"]))
     assert abs(obj - obj_ref) <= obj_tol, (obj, obj_ref)
+    if chaotic:
+        # converged, but to a point of the optimal face that the reference
+        # itself does not pin down: status, iterations and objective are the
+        # defined part
+        return
     tol = max(vec_tol, 10.0 * ref["sens_xdev"])
     for k in ("x", "s", "y"):
         assert rel(out[k], ref[k]) <= tol, (k, rel(out[k], ref[k]), tol)
