@@ -170,6 +170,43 @@ int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m
 void *pdosgpu_batch_stream(pdosgpu_batch *b);
 void pdosgpu_batch_free(pdosgpu_batch *b);
 
+/* ---- learned warm start --------------------------------------------------
+ * A perceptron n_in -> hidden -> hidden -> n_out (ReLU) with BF16 weights
+ * and activations, FP32 accumulation, FP32 master weights and Adam (beta1
+ * 0.9, beta2 0.999, eps 1e-8), trained and run by the library's own tensor-
+ * core kernels.  It maps a problem family's data to a starting iterate for
+ * the solver (the reference's Data.x/y/s, pdos.h:29-32); the solver's
+ * result is always the one reported.  Arrays named x, t, y, mean, stdv,
+ * x0, y0, s0 are DEVICE pointers; parameter arrays of set/get are HOST
+ * arrays of natural shape (W1: hidden x n_in, W2: hidden x hidden,
+ * W3: n_out x hidden, row-major).  The reference has no such component. */
+typedef struct pdosgpu_mlp pdosgpu_mlp;
+
+int pdosgpu_mlp_create(int n_in, int hidden, int n_out, int max_batch, pdosgpu_mlp **out);
+int pdosgpu_mlp_set_params(pdosgpu_mlp *p, const float *w1, const float *b1, const float *w2,
+                           const float *b2, const float *w3, const float *b3);
+/* grads != 0: the gradients of the last training step instead. */
+int pdosgpu_mlp_get_params(pdosgpu_mlp *p, int grads, float *w1, float *b1, float *w2,
+                           float *b2, float *w3, float *b3);
+/* y[batch, n_out] = network(x[batch, n_in]), FP32 in and out. */
+int pdosgpu_mlp_forward(pdosgpu_mlp *p, const float *x, int batch, float *y);
+/* One Adam step on the mean squared error to t[batch, n_out]; batch a
+ * multiple of 8; *loss (host, may be NULL) = the loss before the step. */
+int pdosgpu_mlp_train_step(pdosgpu_mlp *p, const float *x, const float *t, int batch,
+                           float lr, double *loss);
+/* Network output rows [x | y | s] (n + 2m = n_out, standardised) turned
+ * into stacked starting iterates out * stdv + mean: x0[batch*n],
+ * y0[batch*m], s0[batch*m] in double, ready for pdosgpu_batch_warm_start. */
+int pdosgpu_mlp_predict_start(pdosgpu_mlp *p, const float *x, int batch, const float *mean,
+                              const float *stdv, int64_t n, int64_t m, double *x0, double *y0,
+                              double *s0);
+/* Roofline timing of the three forward products on the last inputs:
+ * *ms per forward pass, *flops = 2 * batch * (n_in*h + h*h + h*n_out). */
+int pdosgpu_mlp_time_forward(pdosgpu_mlp *p, int batch, int reps, double *ms, double *flops);
+void *pdosgpu_mlp_stream(pdosgpu_mlp *p);
+int pdosgpu_mlp_sync(pdosgpu_mlp *p);
+void pdosgpu_mlp_free(pdosgpu_mlp *p);
+
 /* pdos() over `count` problems at once: sols[i] is what pdos(d[i], k[i])
  * returns (free each with freeSol), info (may be NULL) gets one record per
  * instance.  Returns PDOSGPU_OK or a negative status (then every sols[i]

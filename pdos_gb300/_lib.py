@@ -92,6 +92,19 @@ SIGNATURES = {
                                     POINTER(c_int64), POINTER(c_int64)]),
     "pdosgpu_batch_stream": (c_void_p, [c_void_p]),
     "pdosgpu_batch_free": (None, [c_void_p]),
+    "pdosgpu_mlp_create": (c_int, [c_int, c_int, c_int, c_int, POINTER(c_void_p)]),
+    "pdosgpu_mlp_set_params": (c_int, [c_void_p] + [c_void_p] * 6),
+    "pdosgpu_mlp_get_params": (c_int, [c_void_p, c_int] + [c_void_p] * 6),
+    "pdosgpu_mlp_forward": (c_int, [c_void_p, c_void_p, c_int, c_void_p]),
+    "pdosgpu_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_float,
+                                       POINTER(c_double)]),
+    "pdosgpu_mlp_predict_start": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_int64,
+                                          c_int64, c_void_p, c_void_p, c_void_p]),
+    "pdosgpu_mlp_time_forward": (c_int, [c_void_p, c_int, c_int, POINTER(c_double),
+                                         POINTER(c_double)]),
+    "pdosgpu_mlp_stream": (c_void_p, [c_void_p]),
+    "pdosgpu_mlp_sync": (c_int, [c_void_p]),
+    "pdosgpu_mlp_free": (None, [c_void_p]),
     "pdos_batch": (c_int, [POINTER(POINTER(Data)), POINTER(POINTER(Cone)), c_int64,
                            POINTER(Options), POINTER(POINTER(Sol)), POINTER(Info)]),
 }
