@@ -1,28 +1,41 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 PDOS indirect solver.
 
-Default workload (single GPU): the factor-model portfolio SOCP with
-n = 200,000 assets, k = 2,000 factors, F at 5 % density (N = 202,001
-variables, m = 404,002 rows, nnz = 20,604,001), FP64, EPS_ABS = 1e-4,
-seeded synthetic data.  One step = one complete solve (reset to the cold
-start, ADMM until the DIMACS test passes).
+Default workload (single GPU): batched solving with a learned warm start on
+the parametrised factor-model portfolio family -- n = 2,000 assets, k = 200
+factors, F at 20 % density shared by the family (N = 2,201 variables,
+m = 4,402 rows, about 86,400 nonzeros per instance); per instance
+mu = mu0 + 0.1 N(0,1) and D scaled entrywise by U[0.8, 1.2]; EPS_ABS 1e-4,
+FP32 storage with FP64 reductions; seeded synthetic data.  The warm-start
+network (4000 -> 1024 -> 1024 -> 11005, BF16) is trained inside the run on
+GPU-solver solutions of a reduced training set (see --train) solved at
+EPS_ABS 1e-5.  One step = one batch of held-out instances (--batch):
+network inference on the device-resident features, warm start, batched
+ADMM until every instance passes the DIMACS test (instances that do not are
+re-solved from the cold start).
 
 JSON line (rank 0):
-  value    solves/s with the problem resident in HBM (device time, CUDA events
-           on the solver's stream), whole job over all ranks
-  e2e      solves/s through the drop-in pdos() with pinned host buffers: H2D
-           of A, b, c, device set-up (transpose, equilibration), solve, D2H of
-           x, s, y -- all inside the timed region
-  roofline the SELL SpMV kernel of the CG A pass (u = A p, the kernel with the
-           largest share of the solve), algorithmic bytes per launch / mean
-           launch time (CUDA events on the solver's stream), against the
-           measured HBM copy peak; traffic from the committed ncu capture
-  cpu_baseline  the oracle (C restatement of the reference, 1 core) on a
-           bounded sample: set-up plus a few ADMM iterations, extrapolated
-           to a full solve with the GPU's iteration count
---impl reference runs that CPU solver instead, on this workload.
-Multi-GPU (torchrun): replicas only -- every rank solves its own copy; no
-collective is involved in the solve.
+  value    solves/s of that step with problem data and features resident in
+           HBM (device time, CUDA events), whole job over all ranks
+  plain_gpu_admm  the same instances solved one at a time by the
+           single-instance GPU engine from the cold start (problem resident)
+  batched_cold    the batch from the cold start, no network
+  e2e      solves/s through the public API with host buffers: batch set-up
+           (H2D of every instance and device set-up), H2D of the features,
+           inference, warm start, solve, D2H of every x, s, y
+  roofline the batch kernel (the whole fused ADMM iteration; all of the
+           solve's device time): algorithmic bytes of the products it ran
+           (values and indices of A and A', pointers, gathered and written
+           vectors) / its device time, against the measured HBM copy peak;
+           the CG products alone are timed beside it (spmv_products)
+  cpu_baseline  the oracle (C restatement of the reference, 1 core) solving
+           a few held-out instances from the cold start
+--impl reference runs that CPU solver on all host cores instead.
+Other workloads (--workload): the single-instance configurations
+(portfolio_n200k_fp64, portfolio_n100_fp64, random_socp_m600k_fp32) and a
+batch of uneven portfolio instances (portfolio_mix_batch).
+Multi-GPU (torchrun): batch workloads shard the instances across ranks (no
+collective); single-instance workloads run replicas.
 """
 import argparse
 import json
@@ -57,7 +70,20 @@ WORKLOADS = {
                                    params=dict(EPS_ABS=1e-4, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4,
                                                MAX_ITERS=2000, NORMALIZE=1)),
 }
-DEFAULT_WORKLOAD = "portfolio_n200k_fp64"
+# batched workloads (many instances per step)
+_BATCH_PARAMS = dict(EPS_ABS=1e-4, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4, MAX_ITERS=4000, NORMALIZE=0)
+BATCH_WORKLOADS = {
+    # parametrised family with the learned warm start (F shared, mu and D
+    # perturbed per instance); the network is trained on a reduced set of
+    # 4,096 GPU solutions at EPS 1e-5 so that the run stays within minutes
+    "portfolio_family_warmstart": dict(kind="family", n=2000, k=200, density=0.2, seed=0,
+                                       precision="fp32", batch=1024, train=4096, train_eps=1e-5,
+                                       epochs=30, hidden=1024, params=_BATCH_PARAMS),
+    # uneven instances: n ~ U[50, 2000], k = ceil(n/10), F at 20 %
+    "portfolio_mix_batch": dict(kind="mix", batch=1024, n_lo=50, n_hi=2000, density=0.2, seed=2,
+                                precision="fp32", params=_BATCH_PARAMS),
+}
+DEFAULT_WORKLOAD = "portfolio_family_warmstart"
 
 
 def make_problem(wl):
@@ -232,13 +258,365 @@ def config_of(args, wl, prob):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+# ================================================================ batches
+BATCH_METRIC = ("solves/s at EPS_ABS 1e-4: batched + learned warm start (one GPU), "
+                "beside plain single-instance GPU ADMM; SpMV HBM GB/s")
+
+
+def batch_draws(wl, count, rank):
+    """The random draws behind this rank's held-out instances (cheap)."""
+    from pdos_gb300 import generators as g
+    if wl["kind"] == "family":
+        fam = g.PortfolioFamily(wl["n"], wl["k"], wl["density"], seed=wl["seed"])
+        mus, ds = fam.draw(count, seed=wl["seed"] + 1000 + rank)
+        return {"fam": fam, "mus": mus, "ds": ds}
+    return {"sizes": g.portfolio_batch_sizes(count, wl["n_lo"], wl["n_hi"], seed=wl["seed"] + rank),
+            "seed": (wl["seed"] + rank) * 1_000_003}
+
+
+def batch_problem(d, wl, i):
+    from pdos_gb300 import generators as g
+    if "fam" in d:
+        return d["fam"].instance(d["mus"][i], d["ds"][i], wl["params"])
+    n, k = d["sizes"][i]
+    return g.portfolio(n, k, wl["density"], seed=d["seed"] + i, params=wl["params"])
+
+
+def batch_instances(wl, count, rank):
+    """(family or None, mus, ds, problems) of this rank's held-out instances."""
+    d = batch_draws(wl, count, rank)
+    probs = [batch_problem(d, wl, i) for i in range(count)]
+    return d.get("fam"), d.get("mus"), d.get("ds"), probs
+
+
+def product_bytes(probs, infos, sv):
+    """Algorithmic bytes of every product a batch solve ran: per instance,
+    A passes = prep + CG + post, A' passes = tops (one more when solved) +
+    CG; each pass reads values and 4-byte indices once, its pointer array,
+    the gathered vector(s) once and writes its result."""
+    total = 0.0
+    for p, d in zip(probs, infos):
+        nnz, m, N = p.nnz, p.m, p.n
+        it, cg = d["admm_iters"], d["cg_iters"]
+        b_ax = nnz * (sv + 4) + (m + 1) * 4 + N * sv + m * sv
+        b_at = nnz * (sv + 4) + (N + 1) * 4 + m * sv + N * sv
+        tops = it + (1 if d["solved"] else 0)
+        total += (1 + cg + it) * b_ax + (cg + tops) * b_at + tops * m * sv  # top gathers y and u
+    return total
+
+
+def cpu_family_sample(probs, count):
+    """Oracle (C restatement of the reference, 1 core) cold solves of the
+    first `count` instances: (solves/s, seconds)."""
+    from oracle import oracle as O
+    O.build_port()
+    t0 = time.perf_counter()
+    for p in probs[:count]:
+        O.port_solve(p)
+    dt = time.perf_counter() - t0
+    return count / dt, dt
+
+
+def _cpu_worker(job):
+    idx, wl_name, count = job
+    wl = BATCH_WORKLOADS[wl_name]
+    from oracle import oracle as O
+    O.port_solve(batch_problem(batch_draws(wl, count, 0), wl, idx))
+    return idx
+
+
+def profile_batch(args, wl):
+    """Profiling case, the kernels of one step: --batch instances (default
+    64); for the family workload an untrained network's inference and the
+    warm start from it; then one launch of the batch kernel running
+    --profile-iters ADMM iterations."""
+    import torch
+    from pdos_gb300 import build
+    build.build()
+    from pdos_gb300.solver import Batch
+    fam, mus, ds, probs = batch_instances(wl, args.batch or 64, 0)
+    with Batch(probs, precision=wl["precision"], iters_per_launch=args.profile_iters) as b:
+        if fam is not None:
+            from pdos_gb300.warmstart import FamilyWarmStart
+            ws = FamilyWarmStart(fam, hidden=wl["hidden"], max_batch=len(probs), seed=0)
+            f = np.concatenate([mus, ds], axis=1)
+            ws.in_mean, ws.in_std = f.mean(axis=0), np.maximum(f.std(axis=0), 1e-12)
+            ws.out_mean = np.zeros(ws.n_out)
+            ws.out_std = np.full(ws.n_out, 1e-3)
+            x0, y0, s0 = ws.predict_device(mus, ds)
+            b.warm_start(x0.data_ptr(), y0.data_ptr(), s0.data_ptr())
+            ws.net.close()
+        b.launch(1)
+        torch.cuda.synchronize()
+        print("instances", len(probs), "iterations", max(d["admm_iters"] for d in b.infos()))
+    return 0
+
+
+def run_batch_reference(args, wl):
+    """--impl reference on a batch workload: the reference's CPU algorithm
+    (the oracle, 1 thread per process) on every host core, one held-out
+    instance per core per step, cold start as the reference has no other."""
+    import multiprocessing as mp
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build_port()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    rates = []
+    with ctx.Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            count = args.batch or wl["batch"]
+            jobs = [((step * cores + j) % count, args.workload, count) for j in range(cores)]
+            t0 = time.perf_counter()
+            pool.map(_cpu_worker, jobs)
+            rates.append(cores / (time.perf_counter() - t0))
+    val = float(np.median(rates[args.warmup:]))
+    line = {
+        "impl": "reference", "metric": BATCH_METRIC, "value": val, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cores / val,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": {"workload": args.workload, "instances_per_step": cores,
+                                                 "params": wl["params"]},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes x 1 held-out instance per step (cold start)"},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_batch(args, wl):
+    import torch
+    ws_n, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if ws_n > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    from pdos_gb300 import build
+    build.build()
+    from pdos_gb300.solver import Batch, Workspace
+    from pdos_gb300.warmstart import FamilyWarmStart, solve_family
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    B = args.batch or wl["batch"]
+    prec = wl["precision"]
+    sv = 8 if prec == "fp64" else 4
+    fam, mus, ds, probs = batch_instances(wl, B, rank)
+    info = {"instances_per_rank": B}
+
+    # ---- learned warm start: training set solved by the GPU batch solver
+    wsn = None
+    if fam is not None:
+        n_train = args.train if args.train is not None else wl["train"]
+        tmus, tds = fam.draw(n_train, seed=wl["seed"] + 11)
+        t0 = time.perf_counter()
+        X, Y, S, tinf = solve_family(fam, tmus, tds, dict(wl["params"], EPS_ABS=wl["train_eps"]), prec)
+        t_data = time.perf_counter() - t0
+        wsn = FamilyWarmStart(fam, hidden=wl["hidden"], max_batch=B, seed=0)
+        t0 = time.perf_counter()
+        hist = wsn.fit(tmus, tds, X, Y, S, epochs=wl["epochs"], batch=256, lr=1e-3)
+        t_fit = time.perf_counter() - t0
+        info["training"] = {"instances": n_train, "eps_abs": wl["train_eps"],
+                            "solved": int(sum(d["solved"] for d in tinf)), "data_seconds": t_data,
+                            "epochs": wl["epochs"], "batch": 256, "fit_seconds": t_fit,
+                            "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1],
+                            "network": f"{wsn.n_in} -> {wl['hidden']} -> {wl['hidden']} -> {wsn.n_out}, "
+                                       "BF16 weights, FP32 accumulation"}
+        del X, Y, S
+
+    batch = Batch(probs, precision=prec, device=local)
+    blocks = batch.tune(4)
+    stream = torch.cuda.ExternalStream(batch.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    # ---- batched cold start (one warm-up, one timed solve)
+    batch.reset().solve()
+    batch.reset()
+    barrier()
+    ev0.record(stream)
+    batch.solve()
+    ev1.record(stream)
+    ev1.synchronize()
+    cold_ms = ev0.elapsed_time(ev1)
+    cold_inf = batch.infos()
+    roof_bytes = product_bytes(probs, cold_inf, sv)
+
+    # ---- the step: inference on resident features, warm start, solve
+    if wsn is not None:
+        feats = torch.from_numpy(wsn.features(mus, ds)).cuda()
+        mean = torch.from_numpy(wsn.out_mean.astype(np.float32)).cuda()
+        std = torch.from_numpy(wsn.out_std.astype(np.float32)).cuda()
+        N, m = wsn.N, wsn.m
+        x0 = torch.empty(B * N, dtype=torch.float64, device="cuda")
+        y0 = torch.empty(B * m, dtype=torch.float64, device="cuda")
+        s0 = torch.empty(B * m, dtype=torch.float64, device="cuda")
+
+    fallbacks = [0]
+
+    def step():
+        if wsn is not None:
+            wsn.net.predict_start(feats, mean, std, N, m, x0, y0, s0)
+            batch.warm_start(x0.data_ptr(), y0.data_ptr(), s0.data_ptr())
+        else:
+            batch.reset()
+        batch.solve()
+        inf = batch.infos()
+        bad = [i for i, d in enumerate(inf) if not d["solved"]]
+        if bad and wsn is not None:  # cold-start fallback
+            fallbacks[0] += len(bad)
+            with Batch([probs[i] for i in bad], precision=prec, device=local) as fb:
+                fb.solve()
+        return inf
+
+    for _ in range(args.warmup):
+        step()
+    launches0 = batch.infos()[0]["kernel_launches"]
+    fallbacks[0] = 0
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            warm_inf = step()
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    dev_ms = ev0.elapsed_time(ev1)
+    launches = batch.infos()[0]["kernel_launches"] - launches0
+    if wsn is not None:
+        launches += args.steps * 6  # conversion, 3 products, scatter, warm-start scaling
+    if pg:
+        t = torch.tensor([dev_ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    value = ws_n * B * args.steps / (dev_ms / 1e3)
+
+    # ---- roofline: the fused batch kernel over the cold solve; products alone
+    peak, peak_kind = measured_peaks()
+    achieved = roof_bytes / (cold_ms / 1e3) / 1e9
+    pm, pb = batch.time_products(4)
+    roofline = {"bound": "hbm", "kernel": "batch_admm_kernel (whole fused ADMM iteration per CTA)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind,
+                "traffic": committed_traffic(args.workload, "batch_admm_kernel"),
+                "algorithmic_bytes_per_solve_of_batch": roof_bytes, "ms_per_solve_of_batch": cold_ms,
+                "spmv_products": {"kernel": "batch_products_kernel (u = A p, t = p + A'u)",
+                                  "achieved": pb / (pm / 1e3) / 1e9, "ms": pm, "bytes": pb,
+                                  "frac": pb / (pm / 1e3) / 1e9 / peak}}
+    if wsn is not None:
+        fms, ffl = wsn.net.time_forward(B, 10)
+        tf_peak = None
+        path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(path):
+            with open(path) as fh:
+                tf_peak = json.load(fh).get("bf16_tflops")
+        roofline["network_forward"] = {"bound": "tensor", "achieved": ffl / (fms / 1e3) / 1e12,
+                                       "unit": "TFLOP/s", "peak": tf_peak, "ms": fms,
+                                       "kernel": "gemm_nt_kernel (mma.sync m16n8k16 BF16)"}
+
+    # ---- plain single-instance GPU ADMM on a few of the same instances
+    plain_n = min(args.plain, B)
+    plain_s, plain_iters = 0.0, []
+    for p in probs[:plain_n]:
+        with Workspace(p, prec, device=local) as w1:
+            w1.solve()  # warm-up
+            w1.reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = w1.solve().fetch()
+            torch.cuda.synchronize()
+            plain_s += time.perf_counter() - t0
+            plain_iters.append(r["iters"])
+    plain = plain_n / plain_s if plain_s > 0 else None
+
+    # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h2d = sum(p.nnz * 16 + (p.n + 1) * 8 + (p.m + p.n) * 8 + len(p.q) * 8 for p in probs)
+        d2h = sum((p.n + 2 * p.m) * 8 for p in probs)
+        if wsn is not None:
+            h2d += B * wsn.n_in * 4
+        e2e_steps = max(1, min(args.steps, 2))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            with Batch(probs, precision=prec, device=local) as eb:
+                eb.set_blocks(blocks)
+                if wsn is not None:
+                    wsn.solve(eb, mus, ds, fallback_params=wl["params"], precision=prec)
+                    eb.fetch_all()
+                else:
+                    eb.solve().fetch_all()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e = {"value": ws_n * B / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s,
+               "path": "pdosgpu_batch_setup from host arrays, features H2D, inference, "
+                       "pdosgpu_batch_warm_start, pdosgpu_batch_solve, pdosgpu_batch_fetch"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, secs = cpu_family_sample(probs, args.cpu_instances)
+        cpu = {"value": rate, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle (C restatement, 1 core): {args.cpu_instances} held-out instances "
+                         f"solved from the cold start in {secs:.1f} s"}
+    if rank == 0:
+        warm_iters = [d["admm_iters"] for d in warm_inf]
+        cold_iters = [d["admm_iters"] for d in cold_inf]
+        cfg = {"workload": args.workload, "instances_per_step": ws_n * B,
+               "nnz_per_step": int(ws_n * sum(p.nnz for p in probs)), "precision": prec,
+               "params": wl["params"], "cta_sizes_by_class": blocks,
+               "l2": "inputs larger than L2: the batch's A and A' (%.0f MB) stream from HBM every "
+                     "iteration (129 MB L2)" % (sum(p.nnz for p in probs) * 2 * (sv + 4) / 1e6),
+               "parallelism": f"instances sharded over {ws_n} GPU(s), no collective"}
+        if fam is not None:
+            cfg.update({"family": {"n": wl["n"], "k": wl["k"], "density": wl["density"]}})
+        line = {
+            "metric": BATCH_METRIC, "value": value, "unit": "solves/s", "n_gpus": ws_n,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 reductions)" if sv == 4 else "f64", "data": "synthetic (seeded)",
+            "config": cfg,
+            "plain_gpu_admm": {"value": plain, "unit": "solves/s", "instances": plain_n,
+                               "admm_iterations_mean": float(np.mean(plain_iters)) if plain_iters else None},
+            "batched_cold": {"value": ws_n * B / (cold_ms / 1e3), "unit": "solves/s",
+                             "admm_iterations_mean": float(np.mean(cold_iters)),
+                             "admm_iterations_max": int(max(cold_iters))},
+            "speedup_vs_plain_gpu_admm": (value / plain) if plain else None,
+            "admm_iterations_mean": float(np.mean(warm_iters)),
+            "admm_iterations_max": int(max(warm_iters)),
+            "solved": int(sum(d["solved"] for d in warm_inf)), "cold_start_fallbacks": fallbacks[0],
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+        }
+        line.update(info)
+        print(json.dumps(line))
+    if wsn is not None:
+        wsn.net.close()
+    batch.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
+    ap.add_argument("--batch", type=int, default=0, help="instances per GPU per step (batch workloads)")
+    ap.add_argument("--train", type=int, default=None, help="training instances (family workload)")
+    ap.add_argument("--plain", type=int, default=8, help="instances solved one at a time for the comparison")
+    ap.add_argument("--cpu-instances", type=int, default=4)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -246,6 +624,13 @@ def main():
                     help="profiling case: set up the workload, run this many ADMM "
                          "iterations, print nothing else (for ncu)")
     args = ap.parse_args()
+    if args.workload in BATCH_WORKLOADS:
+        wl = BATCH_WORKLOADS[args.workload]
+        if args.impl == "reference":
+            return run_batch_reference(args, wl)
+        if args.profile_iters:
+            return profile_batch(args, wl)
+        return run_batch(args, wl)
     wl = WORKLOADS[args.workload]
     prob = make_problem(wl)
     if args.impl == "reference":

@@ -191,6 +191,20 @@ class Batch:
     def stream(self):
         return self.lib.pdosgpu_batch_stream(self._b)
 
+    def infos(self):
+        """Per-instance info dicts only (no solution vectors)."""
+        cnt = len(self.probs)
+        infos = (_lib.Info * cnt)()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _lib.check(self.lib.pdosgpu_batch_fetch(self._b, 0, cnt, dp(), dp(), dp(), infos),
+                   "pdosgpu_batch_fetch", self.lib)
+        out = []
+        for inf in infos:
+            d = inf.as_dict()
+            d["lambda"] = d.pop("lambda_")
+            out.append(d)
+        return out
+
     def fetch_all(self):
         """Stacked x, s, y and a list of per-instance info dicts."""
         cnt = len(self.probs)
