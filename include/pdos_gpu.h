@@ -128,8 +128,11 @@ Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt,
 typedef struct pdosgpu_batch pdosgpu_batch;
 
 /* Set up `count` problems (the work of pdosgpu_setup for each).
- * iters_per_launch: ADMM iterations each instance runs per kernel launch
- * (<= 0: 64); it bounds a launch's duration, not the solve. */
+ * iters_per_launch: ADMM iterations each instance runs per kernel launch;
+ * <= 0 runs every instance to its stop test or MAX_ITERS in one launch, so
+ * that a CTA whose instance finishes takes the next one without waiting for
+ * a launch boundary.  A positive value bounds a launch's duration (results
+ * are identical either way). */
 int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count,
                         const pdosgpu_options *opt, int iters_per_launch,
                         pdosgpu_batch **out);

@@ -18,12 +18,14 @@
 // by operation; only the summation order of the products and reductions
 // differs.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.cuh"
@@ -32,8 +34,15 @@
 namespace pdosgpu {
 namespace batch {
 
-constexpr int kLongRow = 128;  // rows with more nonzeros go to warp-wide pieces
-constexpr int kPiece = 256;    // target nonzeros per piece
+#ifndef PDOS_BATCH_PIECE
+#define PDOS_BATCH_PIECE 1024
+#endif
+#ifndef PDOS_BATCH_UNROLL
+#define PDOS_BATCH_UNROLL 2
+#endif
+constexpr int kLongRow = 128;               // rows with more nonzeros go to warp-wide pieces
+constexpr int kPiece = PDOS_BATCH_PIECE;    // target nonzeros per piece
+constexpr int kUnroll = PDOS_BATCH_UNROLL;  // 16-byte loads in flight per lane and operand
 constexpr int kClasses = 4;    // size classes (by nonzeros per instance)
 constexpr int64_t kClassNnz[kClasses - 1] = {4096, 32768, 262144};
 constexpr int kSmemLimit = 225 * 1024;  // dynamic shared memory per CTA (opt-in limit 227 KB)
@@ -198,7 +207,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     T a0 = T(0), a1 = T(0);
     const int32_t *ip = H.idx + beg;
     const T *vp = H.val + beg;
-#pragma unroll 2
+#pragma unroll kUnroll
     for (int e = 4 * lane; e < len; e += 128) {
       const Idx4 j = ld_stream4(ip + e);
       const Val4<T> v = ld_stream4(vp + e);
@@ -223,7 +232,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     if (width < 0) {  // four columns per lane and load
       const int32_t *ip = H.idx + off + 4 * lane;
       const T *vp = H.val + off + 4 * lane;
-#pragma unroll 2
+#pragma unroll kUnroll
       for (int c4 = 0; c4 < -width; c4 += 4) {
         const Idx4 j = ld_stream4(ip + 32 * c4);
         const Val4<T> v = ld_stream4(vp + 32 * c4);
@@ -580,23 +589,90 @@ __global__ void gather_values_kernel(const int32_t *src, int64_t count, const T 
 }
 
 // ------------------------------------------------------------ host side
+// Work over instances on the host's cores (atomic counter, no exceptions).
+template <class F>
+void parallel_for(int64_t n, F &&f) {
+  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(n, hw));
+  std::atomic<int64_t> next{0};
+  auto body = [&]() {
+    for (int64_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(body);
+  body();
+  for (auto &th : pool) th.join();
+}
+
+// A host array that is not zero-filled on allocation (its writers cover it).
+template <typename T>
+struct Raw {
+  std::unique_ptr<T[]> p;
+  size_t n = 0;
+  void resize(size_t count) {
+    p.reset(count ? new T[count] : nullptr);
+    n = count;
+  }
+  T *data() { return p.get(); }
+  const T *data() const { return p.get(); }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+  T &operator[](size_t i) { return p[i]; }
+  const T &operator[](size_t i) const { return p[i]; }
+  using value_type = T;
+};
+
+// Position in the layout arrays of one side.
+struct Cursor {
+  int64_t slice = 0, piece = 0, split = 0, elem = 0;
+};
+
+// The hybrid layout of one side for every instance.  walk<false> sizes an
+// instance (advances a cursor), walk<true> writes it at a cursor; both make
+// the same decisions, and every instance starts and ends on a multiple of
+// 4 elements, so instances can be sized and written in parallel.
 struct HybBuild {
   std::vector<int64_t> slice_beg;
   std::vector<int32_t> slice_w;
   std::vector<uint32_t> slice_skip;
   std::vector<int32_t> piece_row, piece_len, split_row, split_p0, split_np;
   std::vector<int64_t> piece_beg;
-  std::vector<int32_t> idx, src;  // per element: local gather index, source position
+  Raw<int32_t> idx, src;  // per element: local gather index, source position
+
+  void resize(const Cursor &t) {
+    slice_beg.resize(t.slice);
+    slice_w.resize(t.slice);
+    slice_skip.resize(t.slice);
+    piece_row.resize(t.piece);
+    piece_len.resize(t.piece);
+    piece_beg.resize(t.piece);
+    split_row.resize(t.split);
+    split_p0.resize(t.split);
+    split_np.resize(t.split);
+    idx.resize(t.elem);
+    src.resize(t.elem);
+  }
 
   // Rows [r0, r1) of a row-wise matrix (ptr, gidx absolute); gather indices
   // are made local by subtracting c0.
-  Side add(const int32_t *ptr, const int32_t *gidx, int64_t r0, int64_t r1, int64_t c0) {
+  template <bool WRITE, typename Idx>
+  Side walk(const int32_t *ptr, const Idx *gidx, int64_t r0, int64_t r1, int64_t c0, Cursor &c) {
     Side sd{};
     const int64_t R = r1 - r0;
     sd.rows = (int32_t)R;
-    sd.slice0 = (int64_t)slice_skip.size();
-    sd.piece0 = (int64_t)piece_row.size();
-    sd.split0 = (int64_t)split_row.size();
+    sd.slice0 = c.slice;
+    sd.piece0 = c.piece;
+    sd.split0 = c.split;
+    auto put = [&](int32_t j, int32_t p) {
+      if (WRITE) {
+        idx[c.elem] = j;
+        src[c.elem] = p;
+      }
+      ++c.elem;
+    };
+    auto pad4 = [&]() {
+      while (c.elem % 4) put(0, -1);  // zero entries up to 16-byte alignment
+    };
     for (int64_t s0 = 0; s0 < R; s0 += 32) {
       uint32_t skip = 0;
       int width = 0;
@@ -618,8 +694,11 @@ struct HybBuild {
         width = (width + 3) & ~3;
         pad4();
       }
-      slice_beg.push_back((int64_t)idx.size());
-      slice_w.push_back(vec ? -width : width);
+      if (WRITE) {
+        slice_beg[c.slice] = c.elem;
+        slice_w[c.slice] = vec ? -width : width;
+        slice_skip[c.slice] = skip;
+      }
       for (int cidx = 0; cidx < width; cidx += vec ? 4 : 1) {
         for (int lane = 0; lane < 32; ++lane) {
           for (int t = 0; t < (vec ? 4 : 1); ++t) {
@@ -632,12 +711,11 @@ struct HybBuild {
                 j = (int32_t)(gidx[a + cidx + t] - c0);
               }
             }
-            idx.push_back(j);
-            src.push_back(p);
+            put(j, p);
           }
         }
       }
-      slice_skip.push_back(skip);
+      ++c.slice;
       ++sd.nslices;
     }
     for (int64_t r = 0; r < R; ++r) {
@@ -645,37 +723,66 @@ struct HybBuild {
       if (len <= kLongRow) continue;
       const int64_t np = (len + kPiece - 1) / kPiece;
       if (np > 1) {
-        split_row.push_back((int32_t)r);
-        split_p0.push_back((int32_t)((int64_t)piece_row.size() - sd.piece0));
-        split_np.push_back((int32_t)np);
+        if (WRITE) {
+          split_row[c.split] = (int32_t)r;
+          split_p0[c.split] = (int32_t)(c.piece - sd.piece0);
+          split_np[c.split] = (int32_t)np;
+        }
+        ++c.split;
         ++sd.nsplit;
       }
       for (int64_t k = 0; k < np; ++k) {  // nearly equal pieces
         const int64_t e0 = a + len * k / np, e1 = a + len * (k + 1) / np;
         pad4();
-        piece_row.push_back(np > 1 ? ~(int32_t)r : (int32_t)r);
-        piece_beg.push_back((int64_t)idx.size());
-        for (int64_t e = e0; e < e1; ++e) {
-          idx.push_back((int32_t)(gidx[e] - c0));
-          src.push_back((int32_t)e);
-        }
+        const int64_t beg = c.elem;
+        for (int64_t e = e0; e < e1; ++e) put((int32_t)(gidx[e] - c0), (int32_t)e);
         pad4();
-        piece_len.push_back((int32_t)((int64_t)idx.size() - piece_beg.back()));
+        if (WRITE) {
+          piece_row[c.piece] = np > 1 ? ~(int32_t)r : (int32_t)r;
+          piece_beg[c.piece] = beg;
+          piece_len[c.piece] = (int32_t)(c.elem - beg);
+        }
+        ++c.piece;
         ++sd.npieces;
       }
     }
     pad4();
     return sd;
   }
-
-  // zero entries up to the next multiple of 4 (16-byte alignment)
-  void pad4() {
-    while (idx.size() % 4) {
-      idx.push_back(0);
-      src.push_back(-1);
-    }
-  }
 };
+
+// Sizes every instance, turns the sizes into start cursors, then writes the
+// instances in parallel; side(i) returns (ptr, gidx, r0, r1, c0) of one.
+template <typename Idx, class SideOf>
+void build_layout(HybBuild &hb, int64_t count, SideOf side, std::vector<Side> &out) {
+  std::vector<Cursor> size(count);
+  parallel_for(count, [&](int64_t i) {
+    const int32_t *ptr;
+    const Idx *gidx;
+    int64_t r0, r1, c0;
+    side(i, ptr, gidx, r0, r1, c0);
+    Cursor c;
+    hb.walk<false>(ptr, gidx, r0, r1, c0, c);
+    size[i] = c;
+  });
+  std::vector<Cursor> start(count + 1);
+  for (int64_t i = 0; i < count; ++i) {
+    start[i + 1].slice = start[i].slice + size[i].slice;
+    start[i + 1].piece = start[i].piece + size[i].piece;
+    start[i + 1].split = start[i].split + size[i].split;
+    start[i + 1].elem = start[i].elem + size[i].elem;
+  }
+  hb.resize(start[count]);
+  out.assign(count, Side{});
+  parallel_for(count, [&](int64_t i) {
+    const int32_t *ptr;
+    const Idx *gidx;
+    int64_t r0, r1, c0;
+    side(i, ptr, gidx, r0, r1, c0);
+    Cursor c = start[i];
+    out[i] = hb.walk<true>(ptr, gidx, r0, r1, c0, c);
+  });
+}
 
 template <typename T>
 struct HybDevOwned {
@@ -845,26 +952,23 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   total_nnz = NNZ;
 
   // ---- stacked problem (block diagonal), host
-  std::vector<double> Ax(NNZ), b(M), c(N), x0, y0, s0;
-  std::vector<int64_t> Ai(NNZ), Ap(N + 1);
+  Raw<double> Ax, b, c;
+  Raw<int64_t> Ai, Ap;
+  Ax.resize(NNZ);
+  b.resize(M);
+  c.resize(N);
+  Ai.resize(NNZ);
+  Ap.resize(N + 1);
+  std::vector<double> x0, y0, s0;
   if (any_x) x0.assign(N, 0.0);
   if (any_y) y0.assign(M, 0.0);
   if (any_s) s0.assign(M, 0.0);
   ProblemDesc d;
   {
-    int64_t e = 0;
+    std::vector<int64_t> e0(cnt + 1, 0);  // first nonzero of each instance
     for (int64_t i = 0; i < cnt; ++i) {
       const pdosgpu_problem &p = probs[i];
-      const int64_t nz = p.Ap[p.n];
-      for (int64_t j = 0; j < p.n; ++j) Ap[col0[i] + j] = e + p.Ap[j];
-      if (nz > 0) std::memcpy(&Ax[e], p.Ax, sizeof(double) * nz);
-      for (int64_t k = 0; k < nz; ++k) Ai[e + k] = row0[i] + p.Ai[k];
-      e += nz;
-      std::memcpy(&b[row0[i]], p.b, sizeof(double) * p.m);
-      std::memcpy(&c[col0[i]], p.c, sizeof(double) * p.n);
-      if (p.x0) std::memcpy(&x0[col0[i]], p.x0, sizeof(double) * p.n);
-      if (p.y0) std::memcpy(&y0[row0[i]], p.y0, sizeof(double) * p.m);
-      if (p.s0) std::memcpy(&s0[row0[i]], p.s0, sizeof(double) * p.m);
+      e0[i + 1] = e0[i] + p.Ap[p.n];
       int64_t off = row0[i] + p.f + p.l;
       for (int64_t k = 0; k < p.qsize; ++k) {
         d.soc_off.push_back(off);
@@ -872,7 +976,19 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
         off += p.q[k];
       }
     }
-    Ap[N] = e;
+    parallel_for(cnt, [&](int64_t i) {
+      const pdosgpu_problem &p = probs[i];
+      const int64_t nz = p.Ap[p.n], e = e0[i];
+      for (int64_t j = 0; j < p.n; ++j) Ap[col0[i] + j] = e + p.Ap[j];
+      if (nz > 0) std::memcpy(&Ax[e], p.Ax, sizeof(double) * nz);
+      for (int64_t k = 0; k < nz; ++k) Ai[e + k] = row0[i] + p.Ai[k];
+      std::memcpy(&b[row0[i]], p.b, sizeof(double) * p.m);
+      std::memcpy(&c[col0[i]], p.c, sizeof(double) * p.n);
+      if (p.x0) std::memcpy(&x0[col0[i]], p.x0, sizeof(double) * p.n);
+      if (p.y0) std::memcpy(&y0[row0[i]], p.y0, sizeof(double) * p.m);
+      if (p.s0) std::memcpy(&s0[row0[i]], p.s0, sizeof(double) * p.m);
+    });
+    Ap[N] = e0[cnt];
   }
   d.n = N;
   d.m = M;
@@ -902,12 +1018,11 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   s_init_ = P.s_init;
 
   // ---- hybrid layouts of both sides, instance by instance
-  std::vector<int32_t> Rj(NNZ > 0 ? NNZ : 1), ApI(N + 1);
+  Raw<int32_t> Rj;
+  Rj.resize(NNZ > 0 ? NNZ : 1);
   if (NNZ > 0)
     PDOS_CUDA_TRY(cudaMemcpyAsync(Rj.data(), P.Rj, sizeof(int32_t) * NNZ, cudaMemcpyDeviceToHost, st));
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-  std::vector<int32_t> AiI(NNZ > 0 ? NNZ : 1);
-  for (int64_t k = 0; k < NNZ; ++k) AiI[k] = (int32_t)Ai[k];
   HybBuild bA, bT;
   inst_h_.assign(cnt, Inst{});
   std::vector<int32_t> cone_off_h, cone_len_h;
@@ -930,8 +1045,6 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
       off += p.q[k];
     }
     cone_pos += p.qsize;
-    I.A = bA.add(P.rp_host.data(), Rj.data(), row0[i], row0[i + 1], col0[i]);
-    I.At = bT.add(P.ap_host.data(), AiI.data(), col0[i], col0[i + 1], row0[i]);
     I.lambda = P.lambda[i];
     I.pscale = P.pscale[i];
     I.dscale = P.dscale[i];
@@ -945,6 +1058,30 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     int cls = 0;
     while (cls < kClasses - 1 && nz > kClassNnz[cls]) ++cls;
     I.cls = cls;
+  }
+  {
+    std::vector<Side> sides;
+    const int32_t *rp = P.rp_host.data(), *ap = P.ap_host.data();
+    const int32_t *rj = Rj.data();
+    const int64_t *ai = Ai.data();
+    build_layout<int32_t>(bA, cnt, [&](int64_t i, const int32_t *&ptr, const int32_t *&g, int64_t &r0,
+                                       int64_t &r1, int64_t &c0) {
+      ptr = rp;
+      g = rj;
+      r0 = row0[i];
+      r1 = row0[i + 1];
+      c0 = col0[i];
+    }, sides);
+    for (int64_t i = 0; i < cnt; ++i) inst_h_[i].A = sides[i];
+    build_layout<int64_t>(bT, cnt, [&](int64_t i, const int32_t *&ptr, const int64_t *&g, int64_t &r0,
+                                       int64_t &r1, int64_t &c0) {
+      ptr = ap;
+      g = ai;
+      r0 = col0[i];
+      r1 = col0[i + 1];
+      c0 = row0[i];
+    }, sides);
+    for (int64_t i = 0; i < cnt; ++i) inst_h_[i].At = sides[i];
   }
   PDOS_TRY(hA_.upload(bA, P.Rx, arena_, st));
   PDOS_TRY(hT_.upload(bT, P.Ax, arena_, st));
@@ -1387,7 +1524,7 @@ int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count, const pdosg
   auto w = new (std::nothrow) pdosgpu_batch();
   if (!w) return fail(PDOSGPU_ENOMEM, "host allocation failed");
   int rc = PDOSGPU_OK;
-  if (iters_per_launch <= 0) iters_per_launch = 64;
+  if (iters_per_launch <= 0) iters_per_launch = INT32_MAX;  // each instance runs to its end
   if (o.precision == PDOSGPU_FP32) {
     auto b = std::make_unique<batch::BatchEngine<float>>();
     rc = b->setup(probs, count, o, iters_per_launch);

@@ -130,7 +130,7 @@ class Batch:
     """Many independent problems solved together (pdosgpu_batch_*): one CTA
     per instance at a time, convergence masking, per-instance results."""
 
-    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=64):
+    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0):
         self.lib = _lib.load()
         self.probs = list(probs)
         self._keep = []
