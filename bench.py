@@ -77,10 +77,10 @@ BATCH_WORKLOADS = {
     # perturbed per instance); the network is trained on a reduced set of
     # 4,096 GPU solutions at EPS 1e-5 so that the run stays within minutes
     "portfolio_family_warmstart": dict(kind="family", n=2000, k=200, density=0.2, seed=0,
-                                       precision="fp32", batch=1024, train=4096, train_eps=1e-5,
+                                       precision="fp32", batch=4096, train=4096, train_eps=1e-5,
                                        epochs=30, hidden=1024, params=_BATCH_PARAMS),
     # uneven instances: n ~ U[50, 2000], k = ceil(n/10), F at 20 %
-    "portfolio_mix_batch": dict(kind="mix", batch=1024, n_lo=50, n_hi=2000, density=0.2, seed=2,
+    "portfolio_mix_batch": dict(kind="mix", batch=4096, n_lo=50, n_hi=2000, density=0.2, seed=2,
                                 precision="fp32", params=_BATCH_PARAMS),
 }
 DEFAULT_WORKLOAD = "portfolio_family_warmstart"
@@ -348,7 +348,11 @@ def profile_batch(args, wl):
             ws.net.close()
         b.launch(1)
         torch.cuda.synchronize()
-        print("instances", len(probs), "iterations", max(d["admm_iters"] for d in b.infos()))
+        inf = b.infos()
+        print(json.dumps({"instances": len(probs), "admm_iterations": max(d["admm_iters"] for d in inf),
+                          "cg_iterations": int(sum(d["cg_iters"] for d in inf)),
+                          "algorithmic_bytes_of_launch": product_bytes(
+                              probs, inf, 8 if wl["precision"] == "fp64" else 4)}))
     return 0
 
 
