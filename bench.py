@@ -161,6 +161,16 @@ def committed_traffic(workload, kernel):
     return d.get(workload, {}).get(kernel)
 
 
+def batch_traffic(workload, algorithmic_bytes):
+    """DRAM bytes of the batch kernel over a solve: the committed ncu ratio of
+    DRAM bytes to algorithmic bytes (a smaller launch of the same kernel)
+    times this solve's algorithmic bytes, or None."""
+    d = committed_traffic(workload, "batch_admm_kernel")
+    if not isinstance(d, dict) or "dram_bytes_per_algorithmic_byte" not in d:
+        return None
+    return d["dram_bytes_per_algorithmic_byte"] * algorithmic_bytes
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -509,7 +519,7 @@ def run_batch(args, wl):
     roofline = {"bound": "hbm", "kernel": "batch_admm_kernel (whole fused ADMM iteration per CTA)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind,
-                "traffic": committed_traffic(args.workload, "batch_admm_kernel"),
+                "traffic": batch_traffic(args.workload, roof_bytes),
                 "algorithmic_bytes_per_solve_of_batch": roof_bytes, "ms_per_solve_of_batch": cold_ms,
                 "spmv_products": {"kernel": "batch_products_kernel (u = A p, t = p + A'u)",
                                   "achieved": pb / (pm / 1e3) / 1e9, "ms": pm, "bytes": pb,
