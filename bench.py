@@ -292,11 +292,21 @@ def batch_problem(d, wl, i):
     return g.portfolio(n, k, wl["density"], seed=d["seed"] + i, params=wl["params"])
 
 
-def batch_instances(wl, count, rank):
-    """(family or None, mus, ds, problems) of this rank's held-out instances."""
-    d = batch_draws(wl, count, rank)
-    probs = [batch_problem(d, wl, i) for i in range(count)]
-    return d.get("fam"), d.get("mus"), d.get("ds"), probs
+def batch_instances(wl, count, rank, world=1):
+    """(family or None, mus, ds, problems) of this rank's held-out instances:
+    the shard (pdos_gb300.shard, balanced by nonzeros) of a list of
+    count * world instances."""
+    from pdos_gb300.shard import shard_instances
+    d = batch_draws(wl, count * world, 0)
+    if "fam" in d:
+        costs = [1] * (count * world)
+    else:
+        costs = [n * (3 + wl["density"] * k) + 2 * k for n, k in d["sizes"]]
+    idx = shard_instances(costs, world, rank)
+    probs = [batch_problem(d, wl, i) for i in idx]
+    if "fam" in d:
+        return d["fam"], d["mus"][idx], d["ds"][idx], probs
+    return None, None, None, probs
 
 
 def product_bytes(probs, infos, sv):
@@ -423,7 +433,8 @@ def run_batch(args, wl):
     B = args.batch or wl["batch"]
     prec = wl["precision"]
     sv = 8 if prec == "fp64" else 4
-    fam, mus, ds, probs = batch_instances(wl, B, rank)
+    fam, mus, ds, probs = batch_instances(wl, B, rank, ws_n)
+    B = len(probs)
     info = {"instances_per_rank": B}
 
     # ---- learned warm start: training set solved by the GPU batch solver
