@@ -312,14 +312,15 @@ def batch_instances(wl, count, rank, world=1):
 def product_bytes(probs, infos, sv):
     """Algorithmic bytes of every product a batch solve ran: per instance,
     A passes = prep + CG + post, A' passes = tops (one more when solved) +
-    CG; each pass reads values and 4-byte indices once, its pointer array,
-    the gathered vector(s) once and writes its result."""
+    CG; each pass reads values and indices once (the batch layout's indices
+    are local to an instance and 16-bit), its pointer array, the gathered
+    vector(s) once and writes its result."""
     total = 0.0
     for p, d in zip(probs, infos):
         nnz, m, N = p.nnz, p.m, p.n
         it, cg = d["admm_iters"], d["cg_iters"]
-        b_ax = nnz * (sv + 4) + (m + 1) * 4 + N * sv + m * sv
-        b_at = nnz * (sv + 4) + (N + 1) * 4 + m * sv + N * sv
+        b_ax = nnz * (sv + 2) + (m + 1) * 4 + N * sv + m * sv
+        b_at = nnz * (sv + 2) + (N + 1) * 4 + m * sv + N * sv
         tops = it + (1 if d["solved"] else 0)
         total += (1 + cg + it) * b_ax + (cg + tops) * b_at + tops * m * sv  # top gathers y and u
     return total
@@ -599,7 +600,7 @@ def run_batch(args, wl):
                "nnz_per_step": int(ws_n * sum(p.nnz for p in probs)), "precision": prec,
                "params": wl["params"], "cta_sizes_by_class": blocks,
                "l2": "inputs larger than L2: the batch's A and A' (%.0f MB) stream from HBM every "
-                     "iteration (129 MB L2)" % (sum(p.nnz for p in probs) * 2 * (sv + 4) / 1e6),
+                     "iteration (129 MB L2)" % (sum(p.nnz for p in probs) * 2 * (sv + 2) / 1e6),
                "parallelism": f"instances sharded over {ws_n} GPU(s), no collective"}
         if fam is not None:
             cfg.update({"family": {"n": wl["n"], "k": wl["k"], "density": wl["density"]}})

@@ -83,7 +83,7 @@ struct Hyb {
   const int64_t *piece_beg;
   const int32_t *piece_len;
   const int32_t *split_row, *split_p0, *split_np;  // pieces of each split row
-  const int32_t *idx;          // gather index, local to the instance
+  const uint16_t *idx;         // gather index, local to the instance (< 65,536)
   const T *val;
 };
 
@@ -143,12 +143,10 @@ __device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
 struct Idx4 {
   int x, y, z, w;
 };
-__device__ __forceinline__ Idx4 ld_stream4(const int32_t *p) {
-  Idx4 r;
-  asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-               : "l"(p));
-  return r;
+__device__ __forceinline__ Idx4 ld_stream4(const uint16_t *p) {  // 8-byte aligned
+  unsigned a, b;
+  asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(a), "=r"(b) : "l"(p));
+  return Idx4{(int)(a & 0xffffu), (int)(a >> 16), (int)(b & 0xffffu), (int)(b >> 16)};
 }
 template <typename T>
 struct Val4 {
@@ -205,7 +203,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     const int64_t beg = H.piece_beg[pk];
     const int len = H.piece_len[pk];  // a multiple of 4
     T a0 = T(0), a1 = T(0);
-    const int32_t *ip = H.idx + beg;
+    const uint16_t *ip = H.idx + beg;
     const T *vp = H.val + beg;
 #pragma unroll kUnroll
     for (int e = 4 * lane; e < len; e += 128) {
@@ -230,7 +228,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     const int width = H.slice_w[sk];
     T a0 = T(0), a1 = T(0);
     if (width < 0) {  // four columns per lane and load
-      const int32_t *ip = H.idx + off + 4 * lane;
+      const uint16_t *ip = H.idx + off + 4 * lane;
       const T *vp = H.val + off + 4 * lane;
 #pragma unroll kUnroll
       for (int c4 = 0; c4 < -width; c4 += 4) {
@@ -239,7 +237,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
         fma4<T, NV>(j, v, src0, src1, a0, a1);
       }
     } else {
-      const int32_t *ip = H.idx + off + lane;
+      const uint16_t *ip = H.idx + off + lane;
       const T *vp = H.val + off + lane;
       for (int c = 0; c < width; ++c) {
         const int j = ip[c * 32];
@@ -637,7 +635,8 @@ struct HybBuild {
   std::vector<uint32_t> slice_skip;
   std::vector<int32_t> piece_row, piece_len, split_row, split_p0, split_np;
   std::vector<int64_t> piece_beg;
-  Raw<int32_t> idx, src;  // per element: local gather index, source position
+  Raw<uint16_t> idx;  // per element: local gather index
+  Raw<int32_t> src;   // per element: position of its value in the source array (-1: padding)
 
   void resize(const Cursor &t) {
     slice_beg.resize(t.slice);
@@ -665,7 +664,7 @@ struct HybBuild {
     sd.split0 = c.split;
     auto put = [&](int32_t j, int32_t p) {
       if (WRITE) {
-        idx[c.elem] = j;
+        idx[c.elem] = (uint16_t)j;
         src[c.elem] = p;
       }
       ++c.elem;
@@ -799,7 +798,8 @@ struct HybDevOwned {
     };
     int64_t *slice_beg, *piece_beg;
     uint32_t *slice_skip;
-    int32_t *slice_w, *piece_row, *piece_len, *split_row, *split_p0, *split_np, *idx;
+    int32_t *slice_w, *piece_row, *piece_len, *split_row, *split_p0, *split_np;
+    uint16_t *idx;
     PDOS_TRY(up(&slice_beg, hb.slice_beg));
     PDOS_TRY(up(&slice_w, hb.slice_w));
     PDOS_TRY(up(&slice_skip, hb.slice_skip));
@@ -925,6 +925,11 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     const pdosgpu_problem &p = probs[i];
     const int rc = validate_problem(p);
     if (rc != PDOSGPU_OK) return fail(rc, "instance " + std::to_string(i) + ": " + pdos_gpu_last_error());
+    if (p.m > 65535 || p.n > 65535)
+      return fail(PDOSGPU_ENOTSUP, "instance " + std::to_string(i) +
+                                       " is too large for one CTA's shared memory (m and n must stay "
+                                       "below 65,536 and max(m, n) + m + n + pieces within 225 KB); "
+                                       "solve it with pdosgpu_setup");
     if ((p.normalize != 0) != (probs[0].normalize != 0))
       return fail(PDOSGPU_EINVAL, "all instances of a batch must share NORMALIZE");
     if (p.verbose) {
@@ -1453,8 +1458,8 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
   double b = 0.0;
   for (int64_t i = 0; i < count; ++i) {
     const double sv = sizeof(T), m = inst_h_[i].m, n = inst_h_[i].n, nz = (double)nnz_h_[i];
-    b += nz * (sv + 4) + (m + 1) * 4 + n * sv + m * sv;  // u = A p
-    b += nz * (sv + 4) + (n + 1) * 4 + m * sv + n * sv;  // t = p + A'u
+    b += nz * (sv + 2) + (m + 1) * 4 + n * sv + m * sv;  // u = A p (16-bit indices)
+    b += nz * (sv + 2) + (n + 1) * 4 + m * sv + n * sv;  // t = p + A'u
   }
   auto go = [&](int cls, int block, auto kernel) -> int {
     const size_t sm_bytes = smem_[cls].bytes(sizeof(T));
