@@ -593,6 +593,23 @@ def run_batch(args, wl):
                "path": "pdosgpu_batch_setup from host arrays, features H2D, inference, "
                        "pdosgpu_batch_warm_start, pdosgpu_batch_solve, pdosgpu_batch_fetch"}
 
+    # error of the step's results against the FP64 oracle (the reference's
+    # algorithm solved to a tight tolerance) on a bounded sample
+    oracle_err = None
+    if rank == 0 and not args.no_cpu and args.oracle_instances > 0:
+        from oracle import oracle as O
+        O.build_port()
+        xs = batch.fetch_all()[0]
+        errs, c0, t0 = [], 0, time.perf_counter()
+        tight = dict(EPS_ABS=1e-6, MAX_ITERS=20000, CG_MAX_ITS=40, CG_TOL=1e-8)
+        for p in probs[:args.oracle_instances]:
+            hi = O.port_solve(p.with_params(**tight))
+            oh = float(p.c @ hi["x"])
+            errs.append(abs(float(p.c @ xs[c0:c0 + p.n]) - oh) / max(1.0, abs(oh)))
+            c0 += p.n
+        oracle_err = {"max_relative_objective_error": max(errs), "instances": len(errs),
+                      "oracle": "oracle (C restatement of the reference, FP64) at EPS_ABS 1e-6, "
+                                "CG_MAX_ITS 40, CG_TOL 1e-8", "seconds": time.perf_counter() - t0}
     cpu = None
     if rank == 0 and not args.no_cpu:
         rate, secs = cpu_family_sample(probs, args.cpu_instances)
@@ -625,6 +642,7 @@ def run_batch(args, wl):
             "admm_iterations_mean": float(np.mean(warm_iters)),
             "admm_iterations_max": int(max(warm_iters)),
             "solved": int(sum(d["solved"] for d in warm_inf)), "cold_start_fallbacks": fallbacks[0],
+            "objective_error_vs_fp64_oracle": oracle_err,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk.summary(),
         }
@@ -649,6 +667,8 @@ def main():
     ap.add_argument("--train", type=int, default=None, help="training instances (family workload)")
     ap.add_argument("--plain", type=int, default=8, help="instances solved one at a time for the comparison")
     ap.add_argument("--cpu-instances", type=int, default=4)
+    ap.add_argument("--oracle-instances", type=int, default=2,
+                    help="held-out instances checked against the FP64 oracle (batch workloads)")
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
