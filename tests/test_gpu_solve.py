@@ -9,7 +9,7 @@ reference's sequential sums, so agreement is to rounding, not bit-exact."""
 import numpy as np
 import pytest
 
-from golden_util import VEC_TOL, check_parity, load_case, solve_cases
+from golden_util import VEC_TOL, check_parity, load_case, rel, solve_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -139,3 +139,28 @@ def test_invalid_input_returns_error_and_gpu_stays_usable(built_lib, gpu, bad):
     with pytest.raises(RuntimeError):
         Workspace(p)
     check_parity(prob, ref, solve_problem(prob))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_wide_problem_matches_oracle(built_lib, gpu, port, precision):
+    """A wide matrix (N = 20,201, 260k nonzeros, rows of 1,000 entries): FP64
+    follows the reference's iterates, FP32 reaches its objective."""
+    from pdos_gb300.generators import portfolio
+    from pdos_gb300.solver import solve_problem
+    prob = portfolio(20000, 200, 0.05, seed=5, params=dict(EPS_ABS=5e-3, NORMALIZE=0, VERBOSE=0))
+    ref = port.port_solve(prob)
+    out = solve_problem(prob, precision)
+    assert out["status"] == ref["status"] == "Solved"
+    o_r = float(prob.c @ ref["x"])
+    assert abs(float(prob.c @ out["x"]) - o_r) <= 1e-3 * max(1.0, abs(o_r))
+    if precision == "fp64":
+        assert abs(out["iters"] - ref["iters"]) <= 0.01 * ref["iters"] + 2
+        # CG amplifies a different summation order step by step (to ~1e-9
+        # after 20 steps here, ~3e-5 over the 274-iteration solve); one
+        # iteration with one CG step pins the products themselves
+        for k in ("x", "s", "y"):
+            assert rel(out[k], ref[k]) <= 1e-4, k
+        short = prob.with_params(MAX_ITERS=1, CG_MAX_ITS=1)
+        a, b = solve_problem(short, precision), port.port_solve(short)
+        for k in ("x", "s", "y"):
+            assert rel(a[k], b[k]) <= 1e-12, (k, rel(a[k], b[k]))
