@@ -59,7 +59,6 @@ struct OpPrep {
   T lam;
   DevState *S;
   __device__ bool begin(Ctx &) const { return true; }
-  __device__ const T *src(const Ctx &, int) const { return V.x; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&red)[2]) const {
     const T ax = sum[0], sv = V.s[r], bv = V.b[r], yv = V.y[r];
     V.ax[r] = ax;
@@ -83,7 +82,6 @@ struct OpTop {
   T lam;
   DevState *S;
   __device__ bool begin(Ctx &) const { return !*(volatile int *)&S->done; }
-  __device__ const T *src(const Ctx &, int v) const { return v == 0 ? V.y : V.u; }
   __device__ void row(const Ctx &, int j, const T (&sum)[2], double (&red)[3]) const {
     const T cj = V.c[j];
     const T dr = (cj + sum[0]) / V.E[j];
@@ -129,7 +127,6 @@ struct OpCgA {
   Vecs<T> V;
   DevState *S;
   __device__ bool begin(Ctx &) const { return cg_begin(S); }
-  __device__ const T *src(const Ctx &, int) const { return V.p; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&)[1]) const {
     V.u[r] = sum[0];
   }
@@ -144,7 +141,6 @@ struct OpCgAt {
   Vecs<T> V;
   DevState *S;
   __device__ bool begin(Ctx &) const { return cg_begin(S); }
-  __device__ const T *src(const Ctx &, int) const { return V.u; }
   __device__ void row(const Ctx &, int j, const T (&sum)[1], double (&red)[1]) const {
     const T pj = V.p[j];
     const T tj = pj + sum[0];
@@ -234,7 +230,6 @@ struct OpPost {
   T lam, alpha, one_minus_alpha;
   DevState *S;
   __device__ bool begin(Ctx &) const { return !*(volatile int *)&S->done; }
-  __device__ const T *src(const Ctx &, int) const { return V.x; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&red)[2]) const {
     const T ax = sum[0];
     T stv = V.b[r] + (-ax);
@@ -445,7 +440,6 @@ struct OpAxpy {
   T sc;
   int accum;
   __device__ bool begin(Ctx &) const { return true; }
-  __device__ const T *src(const Ctx &, int) const { return x; }
   __device__ void row(const Ctx &, int r, const T (&sum)[1], double (&)[1]) const {
     const T v = sc * sum[0];
     y[r] = accum ? y[r] + v : v;

@@ -932,9 +932,6 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
                                        "solve it with pdosgpu_setup");
     if ((p.normalize != 0) != (probs[0].normalize != 0))
       return fail(PDOSGPU_EINVAL, "all instances of a batch must share NORMALIZE");
-    if (p.verbose) {
-      // the batch prints nothing per iteration
-    }
     row0.push_back(M);
     col0.push_back(N);
     N += p.n;

@@ -123,7 +123,6 @@ struct DevState {
   long long admm_iter, cg_total;
   int cg_iter, cg_active, done, solved, evaluated;
   int cg_skip;  // done || !cg_active, read by the CG SpMV kernels
-  int error;  // set by a kernel whose bounded wait timed out
 };
 
 }  // namespace pdosgpu
