@@ -552,6 +552,12 @@ def run_batch(args, wl):
         roofline["network_forward"] = {"bound": "tensor", "achieved": ffl / (fms / 1e3) / 1e12,
                                        "unit": "TFLOP/s", "peak": tf_peak, "ms": fms,
                                        "kernel": "gemm_nt_kernel (mma.sync m16n8k16 BF16)"}
+        wsn.net.set_kernel(1)  # the tcgen05 kernel beside it (same results)
+        tms, tfl = wsn.net.time_forward(B, 10)
+        wsn.net.set_kernel(0)
+        roofline["network_forward_tcgen05"] = {"bound": "tensor", "achieved": tfl / (tms / 1e3) / 1e12,
+                                               "unit": "TFLOP/s", "peak": tf_peak, "ms": tms,
+                                               "kernel": "gemm_nt_tc_kernel (tcgen05.mma 128x256x16, TMEM)"}
 
     # ---- plain single-instance GPU ADMM on a few of the same instances
     plain_n = min(args.plain, B)

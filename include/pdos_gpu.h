@@ -207,7 +207,11 @@ int pdosgpu_mlp_predict_start(pdosgpu_mlp *p, const float *x, int batch, const f
  * *ms per forward pass, *flops = 2 * batch * (n_in*h + h*h + h*n_out). */
 int pdosgpu_mlp_time_forward(pdosgpu_mlp *p, int batch, int reps, double *ms, double *flops);
 void *pdosgpu_mlp_stream(pdosgpu_mlp *p);
+/* Waits for the network's stream; fails if a tensor-core product timed out. */
 int pdosgpu_mlp_sync(pdosgpu_mlp *p);
+/* Product kernel: 0 = mma.sync (default), 1 = tcgen05 with tensor-memory
+ * accumulators. */
+int pdosgpu_mlp_set_kernel(pdosgpu_mlp *p, int kind);
 void pdosgpu_mlp_free(pdosgpu_mlp *p);
 
 /* pdos() over `count` problems at once: sols[i] is what pdos(d[i], k[i])

@@ -104,6 +104,7 @@ SIGNATURES = {
                                          POINTER(c_double)]),
     "pdosgpu_mlp_stream": (c_void_p, [c_void_p]),
     "pdosgpu_mlp_sync": (c_int, [c_void_p]),
+    "pdosgpu_mlp_set_kernel": (c_int, [c_void_p, c_int]),
     "pdosgpu_mlp_free": (None, [c_void_p]),
     "pdos_batch": (c_int, [POINTER(POINTER(Data)), POINTER(POINTER(Cone)), c_int64,
                            POINTER(Options), POINTER(POINTER(Sol)), POINTER(Info)]),

@@ -5,12 +5,14 @@
 // warm-start inputs Data.x/y/s, pdos.h:29-32, common.h:147-161); the solver,
 // not the network, produces every reported result.
 //
-// All products go through one tensor-core kernel, C[M,N] = A[M,K] B[N,K]^T
-// with both operands K-contiguous (mma.sync m16n8k16 BF16 -> FP32, ldmatrix
-// fragments, cp.async double buffering), with fused epilogues: bias, ReLU,
-// multiplication by a ReLU mask, BF16 or FP32 output.  The backward pass
-// transposes its operands into that form first.  Every reduction (loss,
-// bias gradients) has a fixed order.
+// Every product is C[M,N] = A[M,K] B[N,K]^T with both operands K-contiguous
+// and a fused epilogue (bias, ReLU, multiplication by a ReLU mask, BF16 or
+// FP32 output), on one of two tensor-core kernels with identical results:
+// mma.sync m16n8k16 (ldmatrix fragments, cp.async double buffering; the
+// default, faster at these sizes) or tcgen05.mma with accumulators in
+// tensor memory (pdosgpu_mlp_set_kernel).  The backward pass transposes its
+// operands into that form first.  Every reduction (loss, bias gradients) has
+// a fixed order.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -144,6 +146,245 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_kernel(const bf16 *__restric
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same product on the 5th-generation tensor cores: one thread issues
+// tcgen05.mma (128 x 256 x 16 per instruction, BF16 in, FP32 accumulators in
+// 256 columns of tensor memory) from shared-memory descriptors; tiles arrive
+// by cp.async, four stages deep, in the canonical no-swizzle K-major layout
+// (8 x 16-byte core matrices, 128 B each); a tcgen05.commit on a per-stage
+// mbarrier tells the loaders when a stage is free; the four warps read the
+// accumulators back with tcgen05.ld (one row per thread) and apply the same
+// epilogue with 16-byte stores.  Every mbarrier wait is bounded: on timeout
+// the kernel records an error flag, stops issuing, and still frees its
+// tensor memory.
+namespace tc {
+constexpr int TM = 128, TN = 256, TK = 32;
+constexpr int kThreads = 128;
+constexpr int kATileBytes = TM * TK * 2;           // 8 KB
+constexpr int kBTileBytes = TN * TK * 2;           // 16 KB
+constexpr int kStageBytes = kATileBytes + kBTileBytes;
+constexpr int kStages = 4;  // 97 KB: two CTAs per SM, 2 x 256 TMEM columns
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // stages + alignment
+constexpr uint32_t kTmemCols = TN;                 // FP32 accumulators: 128 lanes x TN columns
+constexpr long long kWaitCycles = 2000000000ll;  // about one second at 2 GHz
+// instruction descriptor, kind::f16: FP32 accumulate (bit 4), A and B BF16
+// (bits 7, 10), both K-major, N/8 at bit 17, M/16 at bit 24
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                            ((uint32_t)(TM >> 4) << 24);
+
+// shared-memory matrix descriptor, no swizzle: start address, leading
+// (K-direction) and stride (8-row direction) byte offsets, version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// non-blocking probe of an mbarrier phase
+__device__ __forceinline__ bool mbar_test_wait(uint32_t addr, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// true if the phase completed within about a second
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_test_wait(addr, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+
+__global__ void __launch_bounds__(kThreads) gemm_nt_tc_kernel(const bf16 *__restrict__ A, int lda,
+                                                              const bf16 *__restrict__ B, int ldb, int M,
+                                                              int N, int K, Epi ep, int *err) {
+  extern __shared__ unsigned char raw[];
+  __shared__ uint64_t mbar[kStages];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+  unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(base);
+  const uint32_t mb0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
+  if (tid == 0) {
+    s_fail = 0;
+    for (int i = 0; i < kStages; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0 + 8 * i));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  // one 16-byte chunk: row r, K chunk kc of a tile -> core (r/8, kc), row r%8
+  auto load = [&](int stage, int k0) {
+    const uint32_t a_s = sbase + stage * kStageBytes, b_s = a_s + kATileBytes;
+#pragma unroll
+    for (int i = 0; i < (TN * TK / 8) / kThreads; ++i) {  // B rows 0..TN-1, A rows 0..TM-1
+      const int c = tid + i * kThreads;
+      const int r = c / (TK / 8), kc = c % (TK / 8);
+      const uint32_t off = (uint32_t)(((r >> 3) * (TK / 8) + kc) * 128 + (r & 7) * 16);
+      const int gk = k0 + kc * 8;
+      const bool kin = gk < K;
+      const int gb = n0 + r;
+      const bf16 *pb = B + (size_t)(gb < N ? gb : 0) * ldb + (kin ? gk : 0);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(b_s + off), "l"(pb),
+                   "r"((gb < N && kin) ? 16 : 0));
+      if (r < TM) {
+        const int ga = m0 + r;
+        const bf16 *pa = A + (size_t)(ga < M ? ga : 0) * lda + (kin ? gk : 0);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(a_s + off), "l"(pa),
+                     "r"((ga < M && kin) ? 16 : 0));
+      }
+    }
+    asm volatile("cp.async.commit_group;");
+  };
+
+  // Pipeline: tiles 0..kStages-2 in flight first; at step kt the products of
+  // tile kt are issued, then the stage read by tile kt-1 is refilled with
+  // tile kt+kStages-1 once those products have completed (its commit).  Every
+  // completion of every stage's mbarrier is waited for exactly once, in order.
+  const int nk = (K + TK - 1) / TK;
+  bool ok = true;
+  for (int t = 0; t < kStages - 1; ++t) {
+    if (t < nk) load(t, t * TK);
+    else asm volatile("cp.async.commit_group;");  // keep one group per tile
+  }
+  for (int kt = 0; kt < nk; ++kt) {
+    const int st = kt % kStages;
+    asm volatile("cp.async.wait_group %0;" ::"n"(kStages - 2) : "memory");  // tile kt has landed
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async data -> async proxy
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_s = sbase + st * kStageBytes, b_s = a_s + kATileBytes;
+#pragma unroll
+      for (int s = 0; s < TK / 16; ++s) {  // K = 16 per product: two core matrices
+        const uint64_t ad = smem_desc(a_s + s * 256, 128, (TK / 8) * 128);
+        const uint64_t bd = smem_desc(b_s + s * 256, 128, (TK / 8) * 128);
+        const uint32_t acc = (kt > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       mb0 + 8 * st)
+                   : "memory");
+    }
+    const int nxt = kt + kStages - 1;  // tile refilling the stage of tile kt-1
+    if (kt >= 1) {
+      const int pt = kt - 1;
+      if (tid == 0 && !mbar_wait_bounded(mb0 + 8 * (pt % kStages), (uint32_t)((pt / kStages) & 1))) s_fail = 1;
+      __syncthreads();
+      if (s_fail) {
+        ok = false;
+        break;
+      }
+    }
+    if (nxt < nk) load(nxt % kStages, nxt * TK);
+    else asm volatile("cp.async.commit_group;");
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (ok) {  // the last tile's products (the commit covers all earlier ones)
+    const int lt = nk - 1;
+    if (tid == 0 && !mbar_wait_bounded(mb0 + 8 * (lt % kStages), (uint32_t)((lt / kStages) & 1))) s_fail = 1;
+    __syncthreads();
+    ok = !s_fail;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {  // accumulators: warp w holds rows 32w..32w+31 (TMEM lanes)
+    const int r = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < TN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+          "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+          "[%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+            "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+            "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+            "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const int cb = n0 + c0;
+      if (r < M && cb < N) {
+        float x[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
+        const bool full = cb + 32 <= N;  // row chunk in range: 16-byte accesses
+        if (ep.bias) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (full || cb + j < N) x[j] += __ldg(ep.bias + cb + j);
+        }
+        if (ep.relu) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) x[j] = x[j] > 0.f ? x[j] : 0.f;
+        }
+        if (ep.mask) {
+          const bf16 *mrow = ep.mask + (size_t)r * ep.ldm + cb;
+          if (full) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const uint4 w = *reinterpret_cast<const uint4 *>(mrow + 8 * q);
+              const bf16 *h = reinterpret_cast<const bf16 *>(&w);
+#pragma unroll
+              for (int e = 0; e < 8; ++e)
+                if (!(__bfloat162float(h[e]) > 0.f)) x[8 * q + e] = 0.f;
+            }
+          } else {
+            for (int j = 0; j < 32 && cb + j < N; ++j)
+              if (!(__bfloat162float(mrow[j]) > 0.f)) x[j] = 0.f;
+          }
+        }
+        if (ep.out_f32) {
+          float *o = ep.out_f32 + (size_t)r * ep.ldc + cb;
+          if (full) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+              *reinterpret_cast<float4 *>(o + 4 * q) = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+          } else {
+            for (int j = 0; j < 32 && cb + j < N; ++j) o[j] = x[j];
+          }
+        } else {
+          bf16 *o = ep.out_bf16 + (size_t)r * ep.ldc + cb;
+          if (full) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              uint4 w;
+              bf16 *h = reinterpret_cast<bf16 *>(&w);
+#pragma unroll
+              for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16_rn(x[8 * q + e]);
+              *reinterpret_cast<uint4 *>(o + 8 * q) = w;
+            }
+          } else {
+            for (int j = 0; j < 32 && cb + j < N; ++j) o[j] = __float2bfloat16_rn(x[j]);
+          }
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+}  // namespace tc
+
 // out[c, r] = in[r, c] for an R x C block of a BF16 matrix.
 __global__ void transpose_kernel(const bf16 *in, int ldi, bf16 *out, int ldo, int R, int C) {
   __shared__ bf16 tile[32][33];
@@ -264,6 +505,8 @@ class Net {
   int predict_start(const float *x, int B, const float *mean, const float *stdv, int n, int m, double *x0,
                     double *y0, double *s0);
   int time_forward(int B, int reps, double *ms, double *flops);
+  int set_gemm(int kind);
+  int check();
   cudaStream_t stream_ = nullptr;
   int64_t launches = 0;
 
@@ -284,15 +527,41 @@ class Net {
   bf16 *tr_a_ = nullptr, *tr_b_ = nullptr;  // transposed operands of the weight gradients
   float *y_ = nullptr;              // output [B, ld_out] FP32
   double *row_sq_ = nullptr, *loss_d_ = nullptr;
+  int *tc_err_ = nullptr;
+  int gemm_kind_ = 0;
   float *x_stage_ = nullptr;
 };
 
 int Net::gemm(const bf16 *A, int lda, const bf16 *B, int ldb, int M, int N, int K, const Epi &ep) {
   if (M <= 0 || N <= 0) return PDOSGPU_OK;
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  gemm_nt_kernel<<<grid, kThreads, 0, stream_>>>(A, lda, B, ldb, M, N, K, ep);
+  if (gemm_kind_ == 1) {
+    dim3 grid((N + tc::TN - 1) / tc::TN, (M + tc::TM - 1) / tc::TM);
+    tc::gemm_nt_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, stream_>>>(A, lda, B, ldb, M, N, K, ep, tc_err_);
+  } else {
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+    gemm_nt_kernel<<<grid, kThreads, 0, stream_>>>(A, lda, B, ldb, M, N, K, ep);
+  }
   PDOS_CUDA_TRY(cudaGetLastError());
   ++launches;
+  return PDOSGPU_OK;
+}
+
+// 0: mma.sync kernel, 1: tcgen05 kernel.
+int Net::set_gemm(int kind) {
+  if (kind != 0 && kind != 1) return fail(PDOSGPU_EINVAL, "unknown product kernel");
+  if (kind == 1)
+    PDOS_CUDA_TRY(cudaFuncSetAttribute(tc::gemm_nt_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tc::kSmemBytes));
+  gemm_kind_ = kind;
+  return PDOSGPU_OK;
+}
+
+// Nonzero if a tcgen05 product gave up waiting for its tensor cores.
+int Net::check() {
+  int h = 0;
+  PDOS_CUDA_TRY(cudaMemcpyAsync(&h, tc_err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  PDOS_CUDA_TRY(cudaStreamSynchronize(stream_));
+  if (h) return fail(PDOSGPU_ECUDA, "a tensor-core product timed out waiting for its operands");
   return PDOSGPU_OK;
 }
 
@@ -344,6 +613,8 @@ int Net::create(int n_in, int hidden, int n_out, int max_batch) {
   PDOS_TRY(arena_.alloc(&row_sq_, (size_t)max_batch_));
   PDOS_TRY(arena_.alloc(&loss_d_, 1));
   PDOS_TRY(arena_.alloc(&x_stage_, (size_t)max_batch_ * ld_[0]));
+  PDOS_TRY(arena_.alloc(&tc_err_, 1));
+  PDOS_CUDA_TRY(cudaMemsetAsync(tc_err_, 0, sizeof(int), stream_));
   PDOS_CUDA_TRY(cudaStreamSynchronize(stream_));
   return PDOSGPU_OK;
 }
@@ -557,7 +828,12 @@ void *pdosgpu_mlp_stream(pdosgpu_mlp *p) { return p ? p->net.stream_ : nullptr; 
 int pdosgpu_mlp_sync(pdosgpu_mlp *p) {
   if (!p) return fail(PDOSGPU_EINVAL, "NULL network");
   PDOS_CUDA_TRY(cudaStreamSynchronize(p->net.stream_));
-  return PDOSGPU_OK;
+  return p->net.check();
+}
+
+int pdosgpu_mlp_set_kernel(pdosgpu_mlp *p, int kind) {
+  if (!p) return fail(PDOSGPU_EINVAL, "NULL network");
+  return p->net.set_gemm(kind);
 }
 
 void pdosgpu_mlp_free(pdosgpu_mlp *p) { delete p; }

@@ -85,6 +85,11 @@ class Net:
                                                      ctypes.byref(fl)), "pdosgpu_mlp_time_forward", self.lib)
         return ms.value, fl.value
 
+    def set_kernel(self, kind):
+        """0: mma.sync products, 1: tcgen05 products."""
+        _lib.check(self.lib.pdosgpu_mlp_set_kernel(self._p, int(kind)), "pdosgpu_mlp_set_kernel", self.lib)
+        return self
+
     def sync(self):
         _lib.check(self.lib.pdosgpu_mlp_sync(self._p), "pdosgpu_mlp_sync", self.lib)
 

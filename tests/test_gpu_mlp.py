@@ -42,10 +42,14 @@ def _setup(torch, dims, B, seed):
     return net, params, p64, x, t
 
 
-@pytest.mark.parametrize("dims,B", [((40, 64, 64, 37), 24), ((4000, 1024, 1024, 11005), 16)])
-def test_forward_and_gradients_match_oracle(built_lib, torch_cuda, dims, B):
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("dims,B", [((40, 64, 64, 37), 24), ((4000, 1024, 1024, 11005), 16),
+                                    ((200, 256, 256, 300), 264)])
+def test_forward_and_gradients_match_oracle(built_lib, torch_cuda, dims, B, kernel):
+    """kernel 0: mma.sync products; 1: tcgen05 products (tensor memory)."""
     torch = torch_cuda
     net, _, p64, x, t = _setup(torch, dims, B, seed=3)
+    net.set_kernel(kernel)
     xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
     y = torch.empty((B, dims[3]), dtype=torch.float32, device="cuda")
     net.forward(xd, y)
@@ -61,10 +65,12 @@ def test_forward_and_gradients_match_oracle(built_lib, torch_cuda, dims, B):
     net.close()
 
 
-def test_adam_step_matches_oracle(built_lib, torch_cuda):
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_adam_step_matches_oracle(built_lib, torch_cuda, kernel):
     torch = torch_cuda
     dims, B = (40, 64, 64, 37), 24
     net, params, p64, x, t = _setup(torch, dims, B, seed=4)
+    net.set_kernel(kernel)
     xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
     net.train_step(xd, td, 1e-2)
     grads = net.get_params(grads=True)
@@ -75,6 +81,25 @@ def test_adam_step_matches_oracle(built_lib, torch_cuda):
             want, _, _ = M.adam_step(p64[l][k], g, np.zeros_like(g), np.zeros_like(g), 1, 1e-2)
             assert np.allclose(after[l][k], want, rtol=1e-5, atol=1e-6), (l, k)
     net.close()
+
+
+def test_tcgen05_and_mma_sync_products_agree(built_lib, torch_cuda):
+    """The two product kernels give the same forward pass and gradients."""
+    torch = torch_cuda
+    dims, B = (4000, 1024, 1024, 11005), 64
+    outs = []
+    for kernel in (0, 1):
+        net, _, _, x, t = _setup(torch, dims, B, seed=9)
+        net.set_kernel(kernel)
+        xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+        y = torch.empty((B, dims[3]), dtype=torch.float32, device="cuda")
+        net.forward(xd, y)
+        net.train_step(xd, td, 0.0)
+        outs.append((y.cpu().numpy(), net.get_params(grads=True)))
+        net.close()
+    assert relerr(outs[1][0], outs[0][0].astype(np.float64)) <= 1e-5
+    for l in range(3):
+        assert relerr(outs[1][1][l][0], outs[0][1][l][0].astype(np.float64)) <= 1e-3
 
 
 def test_learned_warm_start_beats_cold_start(built_lib, torch_cuda, port):
