@@ -173,7 +173,7 @@ def random_feasible(m=600, n=200, nnz_per_col=20, zero_frac=0.1,
     p = dict(DEFAULT_PARAMS)
     if params:
         p.update(params)
-    return Problem(n, m, Ax, Ai, Ap, b, c, f, l, q, p)
+    return Problem(n, m, Ax, Ai, Ap, b, c, f, l, q, p, optimum={"x": x, "s": s, "y": y})
 
 
 def portfolio_batch_sizes(count, n_lo=50, n_hi=20000, seed=0):

@@ -44,6 +44,9 @@ class Problem:
     x0: np.ndarray = None
     y0: np.ndarray = None
     s0: np.ndarray = None
+    # a known optimal primal-dual pair {'x', 's', 'y'} when the generator
+    # built the problem around one (not part of the file format)
+    optimum: dict = None
 
     @property
     def nnz(self):
@@ -54,12 +57,12 @@ class Problem:
         p.update(kw)
         return Problem(self.n, self.m, self.Ax, self.Ai, self.Ap, self.b,
                        self.c, self.f, self.l, self.q, p, self.x0, self.y0,
-                       self.s0)
+                       self.s0, self.optimum)
 
     def with_warm_start(self, x0=None, y0=None, s0=None):
         return Problem(self.n, self.m, self.Ax, self.Ai, self.Ap, self.b,
                        self.c, self.f, self.l, self.q, dict(self.params),
-                       x0, y0, s0)
+                       x0, y0, s0, self.optimum)
 
     def check(self):
         """Shape and cone-size checks (pdos.c:65-71, pdosmodule.c:94-185)."""
