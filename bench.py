@@ -8,8 +8,8 @@ m = 4,402 rows, about 86,400 nonzeros per instance); per instance
 mu = mu0 + 0.1 N(0,1) and D scaled entrywise by U[0.8, 1.2]; EPS_ABS 1e-4,
 FP32 storage with FP64 reductions; seeded synthetic data.  The warm-start
 network (4000 -> 1024 -> 1024 -> 11005, BF16) is trained inside the run on
-GPU-solver solutions of a reduced training set (see --train) solved at
-EPS_ABS 1e-5.  One step = one batch of held-out instances (--batch):
+GPU-solver solutions of a reduced training set (16,384 instances, --train)
+solved at EPS_ABS 1e-5.  One step = one batch of held-out instances (--batch):
 network inference on the device-resident features, warm start, batched
 ADMM until every instance passes the DIMACS test (instances that do not are
 re-solved from the cold start).
@@ -78,10 +78,10 @@ _BATCH_PARAMS = dict(EPS_ABS=1e-4, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4, MAX_IT
 BATCH_WORKLOADS = {
     # parametrised family with the learned warm start (F shared, mu and D
     # perturbed per instance); the network is trained on a reduced set of
-    # 4,096 GPU solutions at EPS 1e-5 so that the run stays within minutes
+    # 16,384 GPU solutions at EPS 1e-5 so that the run stays within minutes
     "portfolio_family_warmstart": dict(kind="family", n=2000, k=200, density=0.2, seed=0,
-                                       precision="fp32", batch=4096, train=4096, train_eps=1e-5,
-                                       epochs=30, hidden=1024, params=_BATCH_PARAMS),
+                                       precision="fp32", batch=4096, train=16384, train_eps=1e-5,
+                                       epochs=40, hidden=1024, params=_BATCH_PARAMS),
     # uneven instances: n ~ U[50, 2000], k = ceil(n/10), F at 20 %
     "portfolio_mix_batch": dict(kind="mix", batch=4096, n_lo=50, n_hi=2000, density=0.2, seed=2,
                                 precision="fp32", params=_BATCH_PARAMS),

@@ -105,7 +105,7 @@ class Net:
             pass
 
 
-def solve_family(family, mus, ds, params, precision="fp32", chunk=1024, warm=None):
+def solve_family(family, mus, ds, params, precision="fp32", chunk=4096):
     """Solve instances (mus[i], ds[i]) of a PortfolioFamily with the batch
     solver; returns (x [B, N], y [B, m], s [B, m], infos)."""
     from .solver import Batch
