@@ -369,6 +369,7 @@ def profile_batch(args, wl):
         if fam is not None:
             from pdos_gb300.warmstart import FamilyWarmStart
             ws = FamilyWarmStart(fam, hidden=wl["hidden"], max_batch=len(probs), seed=0)
+            ws.net.set_kernel(args.network_kernel)
             f = np.concatenate([mus, ds], axis=1)
             ws.in_mean, ws.in_std = f.mean(axis=0), np.maximum(f.std(axis=0), 1e-12)
             ws.out_mean = np.zeros(ws.n_out)
@@ -676,6 +677,8 @@ def main():
     ap.add_argument("--train", type=int, default=None, help="training instances (family workload)")
     ap.add_argument("--plain", type=int, default=8, help="instances solved one at a time for the comparison")
     ap.add_argument("--cpu-instances", type=int, default=4)
+    ap.add_argument("--network-kernel", type=int, default=0, choices=[0, 1],
+                    help="profiling case: the network's product kernel (0 mma.sync, 1 tcgen05)")
     ap.add_argument("--oracle-instances", type=int, default=2,
                     help="held-out instances checked against the FP64 oracle (batch workloads)")
     ap.add_argument("--cpu-iters", type=int, default=3)
