@@ -454,7 +454,8 @@ def run_batch(args, wl):
         n_train = args.train if args.train is not None else wl["train"]
         tmus, tds = fam.draw(n_train, seed=wl["seed"] + 11)
         t0 = time.perf_counter()
-        X, Y, S, tinf = solve_family(fam, tmus, tds, dict(wl["params"], EPS_ABS=wl["train_eps"]), prec)
+        X, Y, S, tinf = solve_family(fam, tmus, tds, dict(wl["params"], EPS_ABS=wl["train_eps"]), prec,
+                                     device=local)
         t_data = time.perf_counter() - t0
         wsn = FamilyWarmStart(fam, hidden=wl["hidden"], max_batch=B, seed=0)
         t0 = time.perf_counter()
@@ -592,7 +593,7 @@ def run_batch(args, wl):
             with Batch(probs, precision=prec, device=local) as eb:
                 eb.set_blocks(blocks)
                 if wsn is not None:
-                    wsn.solve(eb, mus, ds, fallback_params=wl["params"], precision=prec)
+                    wsn.solve(eb, mus, ds, fallback_params=wl["params"], precision=prec, device=local)
                     eb.fetch_all()
                 else:
                     eb.solve().fetch_all()
@@ -787,12 +788,12 @@ def main():
         p2 = prob.with_params()
         for name, t in pin.items():
             setattr(p2, name, t.numpy())
-        pdos_call(p2, wl["precision"])  # warm-up
+        pdos_call(p2, wl["precision"], device=local)  # warm-up
         barrier()
         t0 = time.perf_counter()
         e2e_steps = max(1, min(args.steps, 3))
         for _ in range(e2e_steps):
-            pdos_call(p2, wl["precision"])
+            pdos_call(p2, wl["precision"], device=local)
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / e2e_steps
         h2d = prob.nnz * 16 + (prob.n + 1) * 8 + prob.m * 8 + prob.n * 8

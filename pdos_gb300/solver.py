@@ -279,15 +279,16 @@ def solve_problem(prob, precision="fp64", scaling="2norm"):
         return ws.solve().fetch()
 
 
-def pdos_call(prob, precision=None, scaling=None, libname="libpdosindir.so"):
-    """Solve through the reference-compatible ``pdos()`` / ``pdos_ex()``."""
+def pdos_call(prob, precision=None, scaling=None, libname="libpdosindir.so", device=None):
+    """Solve through the reference-compatible ``pdos()`` / ``pdos_ex()``
+    (``pdos_ex`` when a precision, scaling or device is given)."""
     lib = _lib.load(libname)
     mar = Marshalled(prob)
-    if precision is None and scaling is None:
+    if precision is None and scaling is None and device is None:
         solp = lib.pdos(ctypes.byref(mar.data), ctypes.byref(mar.cone))
         info = None
     else:
-        opt = make_options(precision or "fp64", scaling or "2norm")
+        opt = make_options(precision or "fp64", scaling or "2norm", device or 0)
         info = _lib.Info()
         solp = lib.pdos_ex(ctypes.byref(mar.data), ctypes.byref(mar.cone), ctypes.byref(opt),
                            ctypes.byref(info))

@@ -105,14 +105,14 @@ class Net:
             pass
 
 
-def solve_family(family, mus, ds, params, precision="fp32", chunk=4096):
+def solve_family(family, mus, ds, params, precision="fp32", chunk=4096, device=0):
     """Solve instances (mus[i], ds[i]) of a PortfolioFamily with the batch
-    solver; returns (x [B, N], y [B, m], s [B, m], infos)."""
+    solver on `device`; returns (x [B, N], y [B, m], s [B, m], infos)."""
     from .solver import Batch
     xs, ys, ss, infos = [], [], [], []
     for c0 in range(0, len(mus), chunk):
         probs = [family.instance(mus[i], ds[i], params) for i in range(c0, min(len(mus), c0 + chunk))]
-        with Batch(probs, precision=precision) as b:
+        with Batch(probs, precision=precision, device=device) as b:
             x, s, y, inf = b.solve().fetch_all()
         N, m = probs[0].n, probs[0].m
         xs.append(x.reshape(-1, N))
@@ -186,7 +186,7 @@ class FamilyWarmStart:
                                    s0[b0 * self.m:b1 * self.m])
         return x0, y0, s0
 
-    def solve(self, batch, mus, ds, fallback_params=None, precision="fp32"):
+    def solve(self, batch, mus, ds, fallback_params=None, precision="fp32", device=0):
         """Warm-start `batch` (a solver.Batch over these instances) from the
         network and solve; instances that do not pass the stop test are
         solved again from the cold start.  Returns (results, stats)."""
@@ -200,7 +200,7 @@ class FamilyWarmStart:
         if failed and fallback_params is not None:
             from .solver import Batch
             probs = [self.family.instance(mus[i], ds[i], fallback_params) for i in failed]
-            with Batch(probs, precision=precision) as cb:
+            with Batch(probs, precision=precision, device=device) as cb:
                 cold = cb.solve().fetch()
             for i, r in zip(failed, cold):
                 r["warm_start"] = "fallback"
