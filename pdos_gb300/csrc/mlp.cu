@@ -13,6 +13,7 @@
 // tensor memory (pdosgpu_mlp_set_kernel).  The backward pass transposes its
 // operands into that form first.  Every reduction (loss, bias gradients) has
 // a fixed order.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -179,23 +180,83 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
 }
 
-// non-blocking probe of an mbarrier phase
-__device__ __forceinline__ bool mbar_test_wait(uint32_t addr, uint32_t parity) {
+// probe of an mbarrier phase (may suspend the thread briefly)
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
       : "r"(addr), "r"(parity)
       : "memory");
   return ok != 0;
 }
 
-// true if the phase completed within about a second
+// true if the phase completed within about a second of clock time
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity) {
   const long long t0 = clock64();
-  while (!mbar_test_wait(addr, parity))
+  while (!mbar_try_wait(addr, parity))
     if (clock64() - t0 > kWaitCycles) return false;
   return true;
+}
+
+// The fused epilogue of one accumulator row chunk (32 columns starting at
+// cb), with 16-byte accesses when the chunk lies inside the matrix.
+__device__ __forceinline__ void store_row32(const Epi &ep, int r, int cb, int M, int N, const uint32_t (&v)[32]) {
+  if (r < M && cb < N) {
+    float x[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
+    const bool full = cb + 32 <= N;  // row chunk in range: 16-byte accesses
+    if (ep.bias) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (full || cb + j < N) x[j] += __ldg(ep.bias + cb + j);
+    }
+    if (ep.relu) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] = x[j] > 0.f ? x[j] : 0.f;
+    }
+    if (ep.mask) {
+      const bf16 *mrow = ep.mask + (size_t)r * ep.ldm + cb;
+      if (full) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint4 w = *reinterpret_cast<const uint4 *>(mrow + 8 * q);
+          const bf16 *h = reinterpret_cast<const bf16 *>(&w);
+#pragma unroll
+          for (int e = 0; e < 8; ++e)
+            if (!(__bfloat162float(h[e]) > 0.f)) x[8 * q + e] = 0.f;
+        }
+      } else {
+        for (int j = 0; j < 32 && cb + j < N; ++j)
+          if (!(__bfloat162float(mrow[j]) > 0.f)) x[j] = 0.f;
+      }
+    }
+    if (ep.out_f32) {
+      float *o = ep.out_f32 + (size_t)r * ep.ldc + cb;
+      if (full) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          *reinterpret_cast<float4 *>(o + 4 * q) = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+      } else {
+        for (int j = 0; j < 32 && cb + j < N; ++j) o[j] = x[j];
+      }
+    } else {
+      bf16 *o = ep.out_bf16 + (size_t)r * ep.ldc + cb;
+      if (full) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint4 w;
+          bf16 *h = reinterpret_cast<bf16 *>(&w);
+#pragma unroll
+          for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16_rn(x[8 * q + e]);
+          *reinterpret_cast<uint4 *>(o + 8 * q) = w;
+        }
+      } else {
+        for (int j = 0; j < 32 && cb + j < N; ++j) o[j] = __float2bfloat16_rn(x[j]);
+      }
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) gemm_nt_tc_kernel(const bf16 *__restrict__ A, int lda,
@@ -319,62 +380,7 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tc_kernel(const bf16 *__rest
             "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      const int cb = n0 + c0;
-      if (r < M && cb < N) {
-        float x[32];
-#pragma unroll
-        for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
-        const bool full = cb + 32 <= N;  // row chunk in range: 16-byte accesses
-        if (ep.bias) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (full || cb + j < N) x[j] += __ldg(ep.bias + cb + j);
-        }
-        if (ep.relu) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) x[j] = x[j] > 0.f ? x[j] : 0.f;
-        }
-        if (ep.mask) {
-          const bf16 *mrow = ep.mask + (size_t)r * ep.ldm + cb;
-          if (full) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const uint4 w = *reinterpret_cast<const uint4 *>(mrow + 8 * q);
-              const bf16 *h = reinterpret_cast<const bf16 *>(&w);
-#pragma unroll
-              for (int e = 0; e < 8; ++e)
-                if (!(__bfloat162float(h[e]) > 0.f)) x[8 * q + e] = 0.f;
-            }
-          } else {
-            for (int j = 0; j < 32 && cb + j < N; ++j)
-              if (!(__bfloat162float(mrow[j]) > 0.f)) x[j] = 0.f;
-          }
-        }
-        if (ep.out_f32) {
-          float *o = ep.out_f32 + (size_t)r * ep.ldc + cb;
-          if (full) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-              *reinterpret_cast<float4 *>(o + 4 * q) = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
-          } else {
-            for (int j = 0; j < 32 && cb + j < N; ++j) o[j] = x[j];
-          }
-        } else {
-          bf16 *o = ep.out_bf16 + (size_t)r * ep.ldc + cb;
-          if (full) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              uint4 w;
-              bf16 *h = reinterpret_cast<bf16 *>(&w);
-#pragma unroll
-              for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16_rn(x[8 * q + e]);
-              *reinterpret_cast<uint4 *>(o + 8 * q) = w;
-            }
-          } else {
-            for (int j = 0; j < 32 && cb + j < N; ++j) o[j] = __float2bfloat16_rn(x[j]);
-          }
-        }
-      }
+      store_row32(ep, r, n0 + c0, M, N, v);
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
@@ -384,6 +390,153 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tc_kernel(const bf16 *__rest
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 }  // namespace tc
+
+// ---------------------------------------------------------------------------
+// The tcgen05 product fed by the Tensor Memory Accelerator: warp-specialised.
+// Thread 0 of warp 0 streams stages with cp.async.bulk.tensor (host-encoded
+// 2-D tensor maps of A and B, zero fill outside the matrices); thread 0 of
+// warp 1 waits for each full stage, issues tcgen05.mma and commits the stage
+// back to the producer; then all four warps drain tensor memory into the
+// epilogue.  A TMA box of 8 K-elements x R rows lands as R rows of 16 bytes,
+// i.e. a column of R/8 core matrices, so the no-swizzle descriptors step
+// 16 B-rows by 128 B (8-row groups) and K-chunks by the box size.
+namespace tma {
+constexpr int TM = 128, TN = 256, TK = 64, KC = TK / 8;
+constexpr int kThreads = 128;
+constexpr int kStages = 3;
+constexpr int kAChunk = TM * 16, kBChunk = TN * 16;  // bytes of one 8-deep K chunk
+constexpr int kABytes = KC * kAChunk, kBBytes = KC * kBChunk;
+constexpr int kStageBytes = kABytes + kBBytes;        // 48 KB
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+constexpr uint32_t kTmemCols = TN;
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                            ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                               const __grid_constant__ CUtensorMap tmB, int M,
+                                                               int N, int K, Epi ep, int *err) {
+  extern __shared__ unsigned char raw[];
+  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+  unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(base);
+  const uint32_t fb = (uint32_t)__cvta_generic_to_shared(&full[0]);
+  const uint32_t eb = (uint32_t)__cvta_generic_to_shared(&empty[0]);
+  const uint32_t db = (uint32_t)__cvta_generic_to_shared(&done);
+  if (tid == 0) {
+    s_fail = 0;
+    for (int i = 0; i < kStages; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fb + 8 * i));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(eb + 8 * i));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(db));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+  }
+  if (warp == 2) {
+    const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const int nk = (K + TK - 1) / TK;
+
+  if (warp == 0) {  // producer: lane 0 streams the stages
+    if (lane == 0) {
+    for (int kt = 0; kt < nk && !*(volatile int *)&s_fail; ++kt) {
+      const int st = kt % kStages;
+      if (kt >= kStages &&
+          !tc::mbar_wait_bounded(eb + 8 * st, (uint32_t)(((kt / kStages) - 1) & 1))) {
+        s_fail = 1;
+        break;
+      }
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb + 8 * st),
+                   "r"((uint32_t)kStageBytes)
+                   : "memory");
+      const uint32_t a_s = sbase + st * kStageBytes, b_s = a_s + kABytes;
+      for (int c = 0; c < KC; ++c) {
+        const int x = kt * TK + 8 * c;  // a multiple of 8 elements: 16-byte aligned
+        tma_load_2d(a_s + c * kAChunk, &tmA, x, m0, fb + 8 * st);
+        tma_load_2d(b_s + c * kBChunk, &tmB, x, n0, fb + 8 * st);
+      }
+    }
+    }
+    __syncwarp();
+  } else if (warp == 1) {  // products: lane 0 issues
+    if (lane == 0) {
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt % kStages;
+      if (!tc::mbar_wait_bounded(fb + 8 * st, (uint32_t)((kt / kStages) & 1))) {
+        s_fail = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_s = sbase + st * kStageBytes, b_s = a_s + kABytes;
+#pragma unroll
+      for (int s = 0; s < TK / 16; ++s) {  // two 8-deep chunks per product
+        const uint64_t ad = tc::smem_desc(a_s + 2 * s * kAChunk, kAChunk, 128);
+        const uint64_t bd = tc::smem_desc(b_s + 2 * s * kBChunk, kBChunk, 128);
+        const uint32_t acc = (kt > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(eb + 8 * st)
+                   : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(db)
+                 : "memory");
+    }
+    __syncwarp();
+  }
+  // everyone: the last commit covers every product
+  bool ok = tc::mbar_wait_bounded(db, 0);
+  __syncthreads();
+  if (s_fail) ok = false;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int r = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < TN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+          "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+          "[%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+            "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+            "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+            "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      tc::store_row32(ep, r, n0 + c0, M, N, v);
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+}  // namespace tma
 
 // out[c, r] = in[r, c] for an R x C block of a BF16 matrix.
 __global__ void transpose_kernel(const bf16 *in, int ldi, bf16 *out, int ldo, int R, int C) {
@@ -507,6 +660,7 @@ class Net {
   int time_forward(int B, int reps, double *ms, double *flops);
   int set_gemm(int kind);
   int check();
+  int encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, int box_rows);
   cudaStream_t stream_ = nullptr;
   int64_t launches = 0;
 
@@ -534,7 +688,13 @@ class Net {
 
 int Net::gemm(const bf16 *A, int lda, const bf16 *B, int ldb, int M, int N, int K, const Epi &ep) {
   if (M <= 0 || N <= 0) return PDOSGPU_OK;
-  if (gemm_kind_ == 1) {
+  if (gemm_kind_ == 2) {
+    CUtensorMap ma, mb;
+    PDOS_TRY(encode_map(&ma, A, lda, M, K, tma::TM));
+    PDOS_TRY(encode_map(&mb, B, ldb, N, K, tma::TN));
+    dim3 grid((N + tma::TN - 1) / tma::TN, (M + tma::TM - 1) / tma::TM);
+    tma::gemm_nt_tma_kernel<<<grid, tma::kThreads, tma::kSmemBytes, stream_>>>(ma, mb, M, N, K, ep, tc_err_);
+  } else if (gemm_kind_ == 1) {
     dim3 grid((N + tc::TN - 1) / tc::TN, (M + tc::TM - 1) / tc::TM);
     tc::gemm_nt_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, stream_>>>(A, lda, B, ldb, M, N, K, ep, tc_err_);
   } else {
@@ -546,13 +706,34 @@ int Net::gemm(const bf16 *A, int lda, const bf16 *B, int ldb, int M, int N, int 
   return PDOSGPU_OK;
 }
 
-// 0: mma.sync kernel, 1: tcgen05 kernel.
+// 0: mma.sync kernel, 1: tcgen05 fed by cp.async, 2: tcgen05 fed by TMA.
 int Net::set_gemm(int kind) {
-  if (kind != 0 && kind != 1) return fail(PDOSGPU_EINVAL, "unknown product kernel");
+  if (kind < 0 || kind > 2) return fail(PDOSGPU_EINVAL, "unknown product kernel");
   if (kind == 1)
     PDOS_CUDA_TRY(cudaFuncSetAttribute(tc::gemm_nt_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        tc::kSmemBytes));
+  if (kind == 2)
+    PDOS_CUDA_TRY(cudaFuncSetAttribute(tma::gemm_nt_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       tma::kSmemBytes));
   gemm_kind_ = kind;
+  return PDOSGPU_OK;
+}
+
+// 2-D tensor map of a row-major BF16 matrix (rows x K, leading dimension
+// ld elements, a multiple of 8): boxes of 8 K-elements x box_rows rows,
+// zero fill outside.
+int Net::encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, int box_rows) {
+  if ((reinterpret_cast<uintptr_t>(p) & 15) || (ld & 7) || K <= 0 || rows <= 0)
+    return fail(PDOSGPU_EINVAL, "tensor-map operand must be 16-byte aligned with ld a multiple of 8");
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
+  const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1u, 1u};
+  const CUresult r = cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(p), dims,
+                                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PDOSGPU_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return PDOSGPU_OK;
 }
 

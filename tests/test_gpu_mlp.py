@@ -42,11 +42,11 @@ def _setup(torch, dims, B, seed):
     return net, params, p64, x, t
 
 
-@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 @pytest.mark.parametrize("dims,B", [((40, 64, 64, 37), 24), ((4000, 1024, 1024, 11005), 16),
                                     ((200, 256, 256, 300), 264)])
 def test_forward_and_gradients_match_oracle(built_lib, torch_cuda, dims, B, kernel):
-    """kernel 0: mma.sync products; 1: tcgen05 products (tensor memory)."""
+    """kernel 0: mma.sync products; 1: tcgen05 fed by cp.async; 2: tcgen05 fed by TMA."""
     torch = torch_cuda
     net, _, p64, x, t = _setup(torch, dims, B, seed=3)
     net.set_kernel(kernel)
@@ -65,7 +65,7 @@ def test_forward_and_gradients_match_oracle(built_lib, torch_cuda, dims, B, kern
     net.close()
 
 
-@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 def test_adam_step_matches_oracle(built_lib, torch_cuda, kernel):
     torch = torch_cuda
     dims, B = (40, 64, 64, 37), 24
@@ -84,11 +84,11 @@ def test_adam_step_matches_oracle(built_lib, torch_cuda, kernel):
 
 
 def test_tcgen05_and_mma_sync_products_agree(built_lib, torch_cuda):
-    """The two product kernels give the same forward pass and gradients."""
+    """The three product kernels give the same forward pass and gradients."""
     torch = torch_cuda
     dims, B = (4000, 1024, 1024, 11005), 64
     outs = []
-    for kernel in (0, 1):
+    for kernel in (0, 1, 2):
         net, _, _, x, t = _setup(torch, dims, B, seed=9)
         net.set_kernel(kernel)
         xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
@@ -97,9 +97,10 @@ def test_tcgen05_and_mma_sync_products_agree(built_lib, torch_cuda):
         net.train_step(xd, td, 0.0)
         outs.append((y.cpu().numpy(), net.get_params(grads=True)))
         net.close()
-    assert relerr(outs[1][0], outs[0][0].astype(np.float64)) <= 1e-5
-    for l in range(3):
-        assert relerr(outs[1][1][l][0], outs[0][1][l][0].astype(np.float64)) <= 1e-3
+    for k in (1, 2):
+        assert relerr(outs[k][0], outs[0][0].astype(np.float64)) <= 1e-5
+        for l in range(3):
+            assert relerr(outs[k][1][l][0], outs[0][1][l][0].astype(np.float64)) <= 1e-3
 
 
 def test_learned_warm_start_beats_cold_start(built_lib, torch_cuda, port):
