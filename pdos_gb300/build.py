@@ -78,7 +78,7 @@ def build(force=False, verbose=False):
         list(ex.map(_compile, units))
     for target, objs in TARGETS.items():
         objs = [os.path.join(OBJ, o) for o in objs if o in present]
-        cmd = [NVCC] + ARCH + ["-shared", "-o", lib_path(target)] + objs + ["-lcuda"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", lib_path(target)] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of {target} failed:\n{r.stderr}")

@@ -729,10 +729,23 @@ int Net::encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, in
   const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
   const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1u, 1u};
-  const CUresult r = cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(p), dims,
-                                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  // The driver entry point is looked up through the runtime, so the library
+  // itself does not link libcuda (it loads on machines without a driver).
+  using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeTiled encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    PDOS_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn)
+      return fail(PDOSGPU_ECUDA, "driver entry point cuTensorMapEncodeTiled not found");
+    encode = reinterpret_cast<EncodeTiled>(fn);
+  }
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(p), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PDOSGPU_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return PDOSGPU_OK;
 }
