@@ -123,8 +123,11 @@ Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt,
  * indirect/private.c:31-118) with its own parameters, lambda, scaling, CG
  * and stop test; one CTA solves one instance at a time and takes the next
  * one when it finishes.  Instances share NORMALIZE; Ruiz scaling is not
- * available for batches.  An instance must fit one CTA's shared memory:
- * max(m, n) + m + n (+ pieces of long rows) values of at most 225 KB. */
+ * available for batches.  m and n of an instance must stay below 65,536
+ * (16-bit instance-local indices).  Instances fall into five classes: four
+ * by nonzeros, whose vectors a CTA stages in shared memory, and one for
+ * instances whose max(m, n) + m + n (+ pieces of long rows) values exceed
+ * 225 KB, staged in a global-memory region of their CTA instead. */
 typedef struct pdosgpu_batch pdosgpu_batch;
 
 /* Set up `count` problems (the work of pdosgpu_setup for each).
@@ -157,7 +160,7 @@ int pdosgpu_batch_fetch(pdosgpu_batch *b, int64_t first, int64_t count, double *
 int64_t pdosgpu_batch_done(pdosgpu_batch *b);
 /* Autotuner: times `iters` iterations of each size class at each CTA size
  * (128, 256, 512), keeps the fastest, resets the batch; blocks (may be
- * NULL) receives the choice for the four classes. */
+ * NULL) receives the choice for the five classes. */
 int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks);
 /* Roofline timing: the two CG products (u = A p, t = p + A'u) of every
  * instance, `reps` times, with nothing else; *ms = device time of the
@@ -165,11 +168,15 @@ int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks);
  * indices of A and A', both pointer arrays, the vector gathered and the
  * vector written, per product).  Leaves the iterate untouched. */
 int pdosgpu_batch_time_products(pdosgpu_batch *b, int reps, double *ms, double *bytes);
-/* Set the CTA size of the four size classes explicitly. */
+/* Set the CTA size of the five size classes explicitly (blocks[5]). */
 int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks);
 /* Number of instances and stacked sizes (any may be NULL). */
 int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m,
                         int64_t *nnz);
+/* Size class of every instance (cls[count]): 0-3 by nonzeros (at most
+ * 4,096 / 32,768 / 262,144 / more), vectors staged in shared memory; 4:
+ * too large for shared memory, vectors staged in global memory. */
+int pdosgpu_batch_classes(pdosgpu_batch *b, int32_t *cls);
 void *pdosgpu_batch_stream(pdosgpu_batch *b);
 void pdosgpu_batch_free(pdosgpu_batch *b);
 

@@ -85,6 +85,7 @@ SIGNATURES = {
     "pdosgpu_batch_warm_start": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "pdosgpu_batch_fetch": (c_int, [c_void_p, c_int64, c_int64, _D, _D, _D, POINTER(Info)]),
     "pdosgpu_batch_done": (c_int64, [c_void_p]),
+    "pdosgpu_batch_classes": (c_int, [c_void_p, c_void_p]),
     "pdosgpu_batch_tune": (c_int, [c_void_p, c_int, POINTER(c_int)]),
     "pdosgpu_batch_set_blocks": (c_int, [c_void_p, POINTER(c_int)]),
     "pdosgpu_batch_time_products": (c_int, [c_void_p, c_int, POINTER(c_double), POINTER(c_double)]),

@@ -43,8 +43,13 @@ namespace batch {
 constexpr int kLongRow = 128;               // rows with more nonzeros go to warp-wide pieces
 constexpr int kPiece = PDOS_BATCH_PIECE;    // target nonzeros per piece
 constexpr int kUnroll = PDOS_BATCH_UNROLL;  // 16-byte loads in flight per lane and operand
-constexpr int kClasses = 4;    // size classes (by nonzeros per instance)
-constexpr int64_t kClassNnz[kClasses - 1] = {4096, 32768, 262144};
+// Size classes: four by nonzeros per instance, whose gather vectors are
+// staged in shared memory, and a fifth for instances too large for one CTA's
+// shared memory, whose vectors are staged in a global-memory region of
+// their CTA instead (L2-resident).
+constexpr int kClasses = 5;
+constexpr int kGlobalClass = 4;
+constexpr int64_t kClassNnz[3] = {4096, 32768, 262144};
 constexpr int kSmemLimit = 225 * 1024;  // dynamic shared memory per CTA (opt-in limit 227 KB)
 constexpr int kBlocks[] = {128, 256, 512};
 constexpr int kNumBlocks = 3;
@@ -99,12 +104,22 @@ struct Dev {
   const T *b, *c, *D, *E;
   Hyb<T> A, At;
   const int32_t *cone_off, *cone_len;  // local first row and size of each cone
+  T *gscratch;  // global staging regions of the global class, one per CTA
 };
 
-// Shared-memory regions of one class, in elements of T.
+// Staging regions of one class, in elements of T: in dynamic shared memory,
+// or (global != 0) in the CTA's region of Dev::gscratch.
 struct Smem {
-  int32_t g1, g2, tt, pb;
-  size_t bytes(size_t elem) const { return elem * ((size_t)g1 + g2 + tt + pb); }
+  int32_t g1, g2, tt, pb, global;
+  __host__ __device__ size_t stride() const {  // elements per CTA region, 128-byte multiples
+    return ((size_t)g1 + g2 + tt + pb + 31) & ~(size_t)31;
+  }
+  size_t need(size_t elem) const { return elem * ((size_t)g1 + g2 + tt + pb); }
+  size_t bytes(size_t elem) const { return global ? 0 : need(elem); }
+  template <typename T>
+  __device__ __forceinline__ T *base(unsigned char *smem_raw, T *gscratch) const {
+    return global ? gscratch + (size_t)blockIdx.x * stride() : reinterpret_cast<T *>(smem_raw);
+  }
 };
 
 template <typename T>
@@ -483,7 +498,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> 
   __shared__ double scratch[3 * (BLOCK / 32)];
   __shared__ Inst s_inst;
   __shared__ int s_k;
-  T *g1 = reinterpret_cast<T *>(smem_raw);
+  T *g1 = sm.base<T>(smem_raw, B.gscratch);
   T *g2 = g1 + sm.g1;
   T *tt = g2 + sm.g2;
   T *pbuf = tt + sm.tt;
@@ -512,7 +527,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Inst s_inst;
   __shared__ int s_k;
-  T *g1 = reinterpret_cast<T *>(smem_raw);
+  T *g1 = sm.base<T>(smem_raw, B.gscratch);
   T *g2 = g1 + sm.g1;
   T *tt = g2 + sm.g2;
   T *pbuf = tt + sm.tt;
@@ -845,6 +860,7 @@ class BatchBase {
                     pdosgpu_info *info) = 0;
   virtual int tune(int iters, int *blocks_out) = 0;
   virtual int time_products(int reps, double *ms, double *bytes) = 0;
+  virtual int instance_class(int64_t i) const = 0;
   virtual int set_blocks(const int *blocks) = 0;
   virtual void *stream() = 0;
   virtual int64_t done_count() = 0;
@@ -879,6 +895,7 @@ class BatchEngine : public BatchBase {
   int tune(int iters, int *blocks_out) override;
   int time_products(int reps, double *ms, double *bytes) override;
   int set_blocks(const int *blocks) override;
+  int instance_class(int64_t i) const override { return inst_h_[i].cls; }
   void *stream() override { return stream_; }
   int64_t done_count() override;
 
@@ -895,6 +912,7 @@ class BatchEngine : public BatchBase {
   std::vector<cudaEvent_t> ev_;
   std::vector<cudaGraphExec_t> exec_;  // [0]: one launch of iter_cap iterations
   int iter_cap_ = 64;
+  int gregions_ = 0;  // staging regions allocated for the global class
   Dev<T> dev_{};
   HybDevOwned<T> hA_, hT_;
   Inst *inst_d_ = nullptr;
@@ -927,9 +945,8 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     if (rc != PDOSGPU_OK) return fail(rc, "instance " + std::to_string(i) + ": " + pdos_gpu_last_error());
     if (p.m > 65535 || p.n > 65535)
       return fail(PDOSGPU_ENOTSUP, "instance " + std::to_string(i) +
-                                       " is too large for one CTA's shared memory (m and n must stay "
-                                       "below 65,536 and max(m, n) + m + n + pieces within 225 KB); "
-                                       "solve it with pdosgpu_setup");
+                                       " is too large for the batch's 16-bit instance-local indices "
+                                       "(m and n must stay below 65,536); solve it with pdosgpu_setup");
     if ((p.normalize != 0) != (probs[0].normalize != 0))
       return fail(PDOSGPU_EINVAL, "all instances of a batch must share NORMALIZE");
     row0.push_back(M);
@@ -1058,7 +1075,7 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     const int64_t nz = p.Ap[p.n];
     nnz_h_.push_back(nz);
     int cls = 0;
-    while (cls < kClasses - 1 && nz > kClassNnz[cls]) ++cls;
+    while (cls < 3 && nz > kClassNnz[cls]) ++cls;
     I.cls = cls;
   }
   {
@@ -1088,8 +1105,15 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   PDOS_TRY(hA_.upload(bA, P.Rx, arena_, st));
   PDOS_TRY(hT_.upload(bT, P.Ax, arena_, st));
 
-  // ---- classes: shared-memory regions and the processing order (largest
-  // instances first within a class)
+  // ---- classes: staging regions and the processing order (largest
+  // instances first within a class); an instance whose own regions exceed
+  // one CTA's shared memory goes to the global class
+  auto r4 = [](int32_t v) { return (v + 3) & ~3; };
+  for (int64_t i = 0; i < cnt; ++i) {
+    Inst &I = inst_h_[i];
+    const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0};
+    if (own.need(sizeof(T)) > (size_t)kSmemLimit) I.cls = kGlobalClass;
+  }
   std::vector<std::vector<int32_t>> members(kClasses);
   for (int64_t i = 0; i < cnt; ++i) members[inst_h_[i].cls].push_back((int32_t)i);
   std::vector<int32_t> order;
@@ -1099,7 +1123,7 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) {
       return probs[a].Ap[probs[a].n] > probs[bb].Ap[probs[bb].n];
     });
-    Smem sm{0, 0, 0, 0};
+    Smem sm{0, 0, 0, 0, k == kGlobalClass ? 1 : 0};
     for (int32_t i : mv) {
       const Inst &I = inst_h_[i];
       sm.g1 = std::max(sm.g1, std::max(I.m, I.n));
@@ -1107,13 +1131,7 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
       sm.tt = std::max(sm.tt, I.n);
       sm.pb = std::max(sm.pb, 2 * std::max(I.A.npieces, I.At.npieces));
     }
-    auto r4 = [](int32_t v) { return (v + 3) & ~3; };
-    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb)};
-    if (sm.bytes(sizeof(T)) > (size_t)kSmemLimit)
-      return fail(PDOSGPU_ENOTSUP, "an instance of the batch is too large for one CTA's shared memory "
-                                   "(max(m, n) + m + n + pieces above " +
-                                   std::to_string(kSmemLimit / sizeof(T)) +
-                                   " values); solve it with pdosgpu_setup");
+    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb), sm.global};
     smem_[k] = sm;
     block_[k] = k == 0 ? 128 : (k == 1 ? 256 : 512);
     order.insert(order.end(), mv.begin(), mv.end());
@@ -1162,6 +1180,12 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   B.At = hT_.h;
   B.cone_off = cone_off_d;
   B.cone_len = cone_len_d;
+  B.gscratch = nullptr;
+  {  // one staging region per resident CTA of the global class (at most 8 per SM)
+    const int members = class_begin_h_[kGlobalClass + 1] - class_begin_h_[kGlobalClass];
+    gregions_ = std::min(members, num_sms() * (1024 / kBlocks[0]));
+    if (gregions_ > 0) PDOS_TRY(arena_.alloc(&B.gscratch, (size_t)gregions_ * smem_[kGlobalClass].stride()));
+  }
   PDOS_TRY(arena_.alloc(&out_, (size_t)N + 2 * (size_t)M));
   PDOS_CUDA_TRY(cudaMallocHost(&host_done_, sizeof(int32_t)));
 
@@ -1193,12 +1217,14 @@ template <typename T>
 int BatchEngine<T>::configure(int cls, int block) {
   const size_t bytes = smem_[cls].bytes(sizeof(T));
   auto go = [&](auto kernel) -> int {
-    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    // one limit for every class that shares this kernel
+    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
     int per_sm = 0;
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, bytes));
     if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "batch kernel does not fit on an SM");
     const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
     grid_[cls] = std::max(1, std::min(members, per_sm * num_sms()));
+    if (smem_[cls].global) grid_[cls] = std::min(grid_[cls], gregions_);
     return PDOSGPU_OK;
   };
   switch (block) {
@@ -1460,12 +1486,13 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
   }
   auto go = [&](int cls, int block, auto kernel) -> int {
     const size_t sm_bytes = smem_[cls].bytes(sizeof(T));
-    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_bytes));
+    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
     int per_sm = 0;
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, sm_bytes));
     if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "product kernel does not fit on an SM");
     const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
-    const int grid = std::max(1, std::min(members, per_sm * num_sms()));
+    int grid = std::max(1, std::min(members, per_sm * num_sms()));
+    if (smem_[cls].global) grid = std::min(grid, gregions_);
     kernel<<<grid, block, sm_bytes, st>>>(dev_, cls, smem_[cls], reps);
     PDOS_CUDA_TRY(cudaGetLastError());
     return PDOSGPU_OK;
@@ -1599,6 +1626,12 @@ int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m
   if (n) *n = b->engine->total_n;
   if (m) *m = b->engine->total_m;
   if (nnz) *nnz = b->engine->total_nnz;
+  return PDOSGPU_OK;
+}
+
+int pdosgpu_batch_classes(pdosgpu_batch *b, int32_t *cls) {
+  if (!b || !b->engine || !cls) return fail(PDOSGPU_EINVAL, "NULL batch or output");
+  for (int64_t i = 0; i < b->engine->count; ++i) cls[i] = b->engine->instance_class(i);
   return PDOSGPU_OK;
 }
 

@@ -167,8 +167,15 @@ class Batch:
     def done(self):
         return int(self.lib.pdosgpu_batch_done(self._b))
 
+    def classes(self):
+        """Size class of each instance: 0-3 by nonzeros, 4 = vectors staged in
+        global memory (too large for one CTA's shared memory)."""
+        out = (ctypes.c_int32 * len(self.probs))()
+        _lib.check(self.lib.pdosgpu_batch_classes(self._b, out), "pdosgpu_batch_classes", self.lib)
+        return list(out)
+
     def tune(self, iters=8):
-        blocks = (ctypes.c_int * 4)()
+        blocks = (ctypes.c_int * 5)()
         _lib.check(self.lib.pdosgpu_batch_tune(self._b, int(iters), blocks), "pdosgpu_batch_tune",
                    self.lib)
         return list(blocks)
@@ -182,7 +189,7 @@ class Batch:
         return ms.value, nb.value
 
     def set_blocks(self, blocks):
-        arr = (ctypes.c_int * 4)(*blocks)
+        arr = (ctypes.c_int * 5)(*blocks)
         _lib.check(self.lib.pdosgpu_batch_set_blocks(self._b, arr), "pdosgpu_batch_set_blocks",
                    self.lib)
         return self

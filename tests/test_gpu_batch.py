@@ -6,7 +6,8 @@ golden cases run as two batches (one per NORMALIZE value) and each result is
 held to its golden with check_parity.  Uneven portfolio instances that reach
 every size class, the CTA-wide cone path (cones above 1024 rows) and split
 rows (above 256 nonzeros) are compared with the single-instance GPU solver
-and with the oracle.  The rest pins the batch mechanics: results do not
+and with the oracle, and so are instances too large for one CTA's shared
+memory (vectors staged in global memory).  The rest pins the batch mechanics: results do not
 depend on how many iterations a launch runs, repeated solves are
 bit-identical, device warm starts equal set-up warm starts, and the C entry
 point pdos_batch returns what the Python wrapper returns."""
@@ -109,6 +110,55 @@ def test_fp32_batch_reaches_fp64_oracle(built_lib, torch_cuda, port):
         assert abs(float(p.c @ out["x"]) - o_hi) <= 1e-3 * max(1.0, abs(o_hi)), i
 
 
+def _oversize_batch():
+    """Instances whose vectors do not fit one CTA's shared memory in FP64
+    (staged in global memory), between ordinary ones."""
+    from pdos_gb300 import generators as g
+    P = dict(EPS_ABS=1e-4, VERBOSE=0, MAX_ITERS=3000)
+    return [g.portfolio(100, 10, 0.5, seed=5, params=P),
+            g.portfolio(6000, 60, 0.05, seed=6, params=P),
+            g.random_feasible(m=30000, n=50, nnz_per_col=40, zero_frac=0.1, nonneg_frac=0.4, seed=7,
+                              params=P),
+            g.portfolio(400, 40, 0.2, seed=8, params=P)]
+
+
+def test_oversize_instances_match_single_instance_solves(built_lib, torch_cuda):
+    from pdos_gb300.solver import Batch, solve_problem
+    probs = _oversize_batch()
+    with Batch(probs) as b:
+        classes = b.classes()
+        outs = b.solve().fetch()
+        again = b.reset().solve().fetch()
+    assert classes[1] == classes[2] == 4 and classes[0] < 4 and classes[3] < 4, classes
+    for i, (p, out) in enumerate(zip(probs, outs)):
+        single = solve_problem(p)
+        assert out["status"] == single["status"], i
+        assert abs(out["iters"] - single["iters"]) <= max(3, 0.02 * single["iters"]), \
+            (i, out["iters"], single["iters"])
+        o_b, o_s = float(p.c @ out["x"]), float(p.c @ single["x"])
+        assert abs(o_b - o_s) <= 1e-5 * max(1.0, abs(o_s)), (i, o_b, o_s)
+        for k in ("x", "s", "y"):
+            assert rel(out[k], single[k]) <= 1e-4, (i, k, rel(out[k], single[k]))
+            assert np.array_equal(out[k], again[i][k]), (i, k)
+
+
+def test_oversize_fp32_batch_reaches_fp64_oracle(built_lib, torch_cuda, port):
+    from pdos_gb300 import generators as g
+    from pdos_gb300.solver import Batch
+    P = dict(EPS_ABS=1e-4, VERBOSE=0, MAX_ITERS=3000)
+    probs = [g.portfolio(12000, 40, 0.02, seed=9, params=P), g.portfolio(80, 8, 0.5, seed=10, params=P)]
+    with Batch(probs, precision="fp32") as b:
+        classes = b.classes()
+        outs = b.solve().fetch()
+    assert classes[0] == 4 and classes[1] < 4, classes
+    for i, (p, out) in enumerate(zip(probs, outs)):
+        hi = port.port_solve(p.with_params(EPS_ABS=1e-7, MAX_ITERS=20000, CG_MAX_ITS=60,
+                                           CG_TOL=1e-12))
+        assert out["status"] == "Solved", i
+        o_hi = float(p.c @ hi["x"])
+        assert abs(float(p.c @ out["x"]) - o_hi) <= 1e-3 * max(1.0, abs(o_hi)), i
+
+
 def test_results_do_not_depend_on_iterations_per_launch(built_lib, torch_cuda):
     from pdos_gb300.solver import Batch
     probs = _uneven_portfolios()[:5]
@@ -186,9 +236,9 @@ def test_batch_rejects_what_it_cannot_run(built_lib, torch_cuda):
     b = g.portfolio(50, 5, 0.5, seed=2, params=dict(NORMALIZE=1, VERBOSE=0))
     with pytest.raises(RuntimeError, match="NORMALIZE"):
         Batch([a, b])
-    big = g.random_feasible(m=40000, n=2, nnz_per_col=3, zero_frac=1.0, nonneg_frac=0.0, seed=3,
+    big = g.random_feasible(m=70000, n=2, nnz_per_col=3, zero_frac=1.0, nonneg_frac=0.0, seed=3,
                             params=dict(VERBOSE=0))
-    with pytest.raises(RuntimeError, match="shared memory"):
+    with pytest.raises(RuntimeError, match="16-bit"):
         Batch([a, big])
     # the GPU stays usable
     with Batch([a]) as ok:
