@@ -592,9 +592,8 @@ def run_batch(args, wl):
         for _ in range(e2e_steps):
             with Batch(probs, precision=prec, device=local) as eb:
                 eb.set_blocks(blocks)
-                if wsn is not None:
+                if wsn is not None:  # fetches every result once
                     wsn.solve(eb, mus, ds, fallback_params=wl["params"], precision=prec, device=local)
-                    eb.fetch_all()
                 else:
                     eb.solve().fetch_all()
         torch.cuda.synchronize()

@@ -116,11 +116,16 @@ struct Smem {
   }
   size_t need(size_t elem) const { return elem * ((size_t)g1 + g2 + tt + pb); }
   size_t bytes(size_t elem) const { return global ? 0 : need(elem); }
-  template <typename T>
-  __device__ __forceinline__ T *base(unsigned char *smem_raw, T *gscratch) const {
-    return global ? gscratch + (size_t)blockIdx.x * stride() : reinterpret_cast<T *>(smem_raw);
-  }
 };
+
+// Base of a CTA's staging regions.  A compile-time choice, so that kernels
+// staging in shared memory keep shared-memory gathers (a pointer that may
+// point to either space turns every gather into a generic load).
+template <typename T, bool GLOBAL>
+__device__ __forceinline__ T *staging_base(const Smem &sm, unsigned char *smem_raw, T *gscratch) {
+  if (GLOBAL) return gscratch + (size_t)blockIdx.x * sm.stride();
+  return reinterpret_cast<T *>(smem_raw);
+}
 
 template <typename T>
 __device__ __forceinline__ T warp_sum_t(T v) {
@@ -492,13 +497,13 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
   }
 }
 
-template <typename T, int BLOCK>
+template <typename T, int BLOCK, bool GLOBAL>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double scratch[3 * (BLOCK / 32)];
   __shared__ Inst s_inst;
   __shared__ int s_k;
-  T *g1 = sm.base<T>(smem_raw, B.gscratch);
+  T *g1 = staging_base<T, GLOBAL>(sm, smem_raw, B.gscratch);
   T *g2 = g1 + sm.g1;
   T *tt = g2 + sm.g2;
   T *pbuf = tt + sm.tt;
@@ -521,13 +526,13 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> 
 // The two CG products alone (u = A p, t = p + A'u), `reps` times for every
 // instance of a class, for the roofline of the batch's SpMV: no reductions,
 // no stop test, the iterate untouched (p is the current x).
-template <typename T, int BLOCK>
+template <typename T, int BLOCK, bool GLOBAL>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev<T> B, int cls, Smem sm,
                                                                               int reps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Inst s_inst;
   __shared__ int s_k;
-  T *g1 = sm.base<T>(smem_raw, B.gscratch);
+  T *g1 = staging_base<T, GLOBAL>(sm, smem_raw, B.gscratch);
   T *g2 = g1 + sm.g1;
   T *tt = g2 + sm.g2;
   T *pbuf = tt + sm.tt;
@@ -848,6 +853,30 @@ struct HybDevOwned {
 inline double now_ms() {
   using namespace std::chrono;
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T>
+using KernelOf = void (*)(Dev<T>, int, Smem, int);
+
+// The persistent ADMM kernel and the product timing kernel of one CTA size,
+// staging in shared or in global memory (nullptr: unsupported size).
+template <typename T>
+KernelOf<T> admm_kernel_for(int block, bool global) {
+  switch (block) {
+    case 128: return global ? batch_admm_kernel<T, 128, true> : batch_admm_kernel<T, 128, false>;
+    case 256: return global ? batch_admm_kernel<T, 256, true> : batch_admm_kernel<T, 256, false>;
+    case 512: return global ? batch_admm_kernel<T, 512, true> : batch_admm_kernel<T, 512, false>;
+    default: return nullptr;
+  }
+}
+template <typename T>
+KernelOf<T> products_kernel_for(int block, bool global) {
+  switch (block) {
+    case 128: return global ? batch_products_kernel<T, 128, true> : batch_products_kernel<T, 128, false>;
+    case 256: return global ? batch_products_kernel<T, 256, true> : batch_products_kernel<T, 256, false>;
+    case 512: return global ? batch_products_kernel<T, 512, true> : batch_products_kernel<T, 512, false>;
+    default: return nullptr;
+  }
 }
 
 class BatchBase {
@@ -1227,24 +1256,18 @@ int BatchEngine<T>::configure(int cls, int block) {
     if (smem_[cls].global) grid_[cls] = std::min(grid_[cls], gregions_);
     return PDOSGPU_OK;
   };
-  switch (block) {
-    case 128: return go(batch_admm_kernel<T, 128>);
-    case 256: return go(batch_admm_kernel<T, 256>);
-    case 512: return go(batch_admm_kernel<T, 512>);
-    default: return fail(PDOSGPU_EINVAL, "unsupported CTA size");
-  }
+  auto kernel = admm_kernel_for<T>(block, smem_[cls].global != 0);
+  if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+  return go(kernel);
 }
 
 template <typename T>
 int BatchEngine<T>::launch_class(int cls, int block, int iter_cap, cudaStream_t st) {
   const Smem sm = smem_[cls];
   const size_t bytes = sm.bytes(sizeof(T));
-  switch (block) {
-    case 128: batch_admm_kernel<T, 128><<<grid_[cls], 128, bytes, st>>>(dev_, cls, sm, iter_cap); break;
-    case 256: batch_admm_kernel<T, 256><<<grid_[cls], 256, bytes, st>>>(dev_, cls, sm, iter_cap); break;
-    case 512: batch_admm_kernel<T, 512><<<grid_[cls], 512, bytes, st>>>(dev_, cls, sm, iter_cap); break;
-    default: return fail(PDOSGPU_EINVAL, "unsupported CTA size");
-  }
+  auto kernel = admm_kernel_for<T>(block, sm.global != 0);
+  if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+  kernel<<<grid_[cls], block, bytes, st>>>(dev_, cls, sm, iter_cap);
   PDOS_CUDA_TRY(cudaGetLastError());
   return PDOSGPU_OK;
 }
@@ -1501,11 +1524,9 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
     PDOS_CUDA_TRY(cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st));
     for (int k = 0; k < kClasses; ++k) {
       if (class_begin_h_[k + 1] == class_begin_h_[k]) continue;
-      switch (block_[k]) {
-        case 128: PDOS_TRY(go(k, 128, batch_products_kernel<T, 128>)); break;
-        case 256: PDOS_TRY(go(k, 256, batch_products_kernel<T, 256>)); break;
-        default: PDOS_TRY(go(k, 512, batch_products_kernel<T, 512>)); break;
-      }
+      auto kernel = products_kernel_for<T>(block_[k], smem_[k].global != 0);
+      if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+      PDOS_TRY(go(k, block_[k], kernel));
     }
     launches += kClasses;
     return PDOSGPU_OK;
