@@ -159,7 +159,7 @@ int pdosgpu_batch_fetch(pdosgpu_batch *b, int64_t first, int64_t count, double *
 /* Instances finished so far (negative on error). */
 int64_t pdosgpu_batch_done(pdosgpu_batch *b);
 /* Autotuner: times `iters` iterations of each size class at each CTA size
- * (128, 256, 512), keeps the fastest, resets the batch; blocks (may be
+ * (128, 256, 512, 1024), keeps the fastest, resets the batch; blocks (may be
  * NULL) receives the choice for the five classes. */
 int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks);
 /* Roofline timing: the two CG products (u = A p, t = p + A'u) of every

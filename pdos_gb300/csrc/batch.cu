@@ -51,8 +51,8 @@ constexpr int kClasses = 5;
 constexpr int kGlobalClass = 4;
 constexpr int64_t kClassNnz[3] = {4096, 32768, 262144};
 constexpr int kSmemLimit = 225 * 1024;  // dynamic shared memory per CTA (opt-in limit 227 KB)
-constexpr int kBlocks[] = {128, 256, 512};
-constexpr int kNumBlocks = 3;
+constexpr int kBlocks[] = {128, 256, 512, 1024};
+constexpr int kNumBlocks = 4;
 
 // One side (A: rows of A; At: rows of A', i.e. columns of A) of an instance
 // in the hybrid layout: slices of 32 consecutive rows stored column-major
@@ -866,6 +866,7 @@ KernelOf<T> admm_kernel_for(int block, bool global) {
     case 128: return global ? batch_admm_kernel<T, 128, true> : batch_admm_kernel<T, 128, false>;
     case 256: return global ? batch_admm_kernel<T, 256, true> : batch_admm_kernel<T, 256, false>;
     case 512: return global ? batch_admm_kernel<T, 512, true> : batch_admm_kernel<T, 512, false>;
+    case 1024: return global ? batch_admm_kernel<T, 1024, true> : batch_admm_kernel<T, 1024, false>;
     default: return nullptr;
   }
 }
@@ -875,6 +876,7 @@ KernelOf<T> products_kernel_for(int block, bool global) {
     case 128: return global ? batch_products_kernel<T, 128, true> : batch_products_kernel<T, 128, false>;
     case 256: return global ? batch_products_kernel<T, 256, true> : batch_products_kernel<T, 256, false>;
     case 512: return global ? batch_products_kernel<T, 512, true> : batch_products_kernel<T, 512, false>;
+    case 1024: return global ? batch_products_kernel<T, 1024, true> : batch_products_kernel<T, 1024, false>;
     default: return nullptr;
   }
 }
@@ -1429,7 +1431,7 @@ int BatchEngine<T>::set_blocks(const int *blocks) {
   for (int k = 0; k < kClasses; ++k) {
     bool ok = false;
     for (int j = 0; j < kNumBlocks; ++j) ok |= blocks[k] == kBlocks[j];
-    if (!ok) return fail(PDOSGPU_EINVAL, "CTA sizes must be 128, 256 or 512");
+    if (!ok) return fail(PDOSGPU_EINVAL, "CTA sizes must be 128, 256, 512 or 1024");
   }
   for (int k = 0; k < kClasses; ++k) block_[k] = blocks[k];
   if (exec_[0]) cudaGraphExecDestroy(exec_[0]);
