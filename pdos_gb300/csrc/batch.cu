@@ -9,7 +9,10 @@
 // (cones.c:21-47).  The vector a product gathers from is staged in shared
 // memory, so the matrix streams from HBM with coalesced loads while the
 // random gathers hit shared memory; CG's p, A p and t never leave shared
-// memory.  A finished instance frees its CTA for the next one (convergence
+// memory.  An instance whose vectors do not fit one CTA's shared memory
+// stages them in a global-memory region of its CTA instead (a separate
+// kernel instantiation, so that the shared-memory kernels keep
+// shared-memory gathers).  A finished instance frees its CTA for the next one (convergence
 // masking), every reduction has a fixed order, and the kernel of one launch
 // runs each instance for at most `iter_cap` iterations, so a captured launch
 // can be replayed until every instance is done.
