@@ -556,13 +556,14 @@ def run_batch(args, wl):
                 tf_peak = json.load(fh).get("bf16_tflops")
         roofline["network_forward"] = {"bound": "tensor", "achieved": ffl / (fms / 1e3) / 1e12,
                                        "unit": "TFLOP/s", "peak": tf_peak, "ms": fms,
-                                       "kernel": "gemm_nt_kernel (mma.sync m16n8k16 BF16)"}
-        wsn.net.set_kernel(2)  # the TMA-fed tcgen05 kernel beside it (same results)
+                                       "kernel": "gemm_nt_tma_kernel (TMA 128-byte swizzled tiles, "
+                                                 "tcgen05.mma 128x256x16, TMEM accumulators)"}
+        wsn.net.set_kernel(0)  # the mma.sync kernel beside it (same results)
         tms, tfl = wsn.net.time_forward(B, 10)
-        wsn.net.set_kernel(0)
-        roofline["network_forward_tcgen05"] = {"bound": "tensor", "achieved": tfl / (tms / 1e3) / 1e12,
-                                               "unit": "TFLOP/s", "peak": tf_peak, "ms": tms,
-                                               "kernel": "gemm_nt_tma_kernel (TMA + tcgen05.mma 128x256x16, TMEM)"}
+        wsn.net.set_kernel(2)
+        roofline["network_forward_mma_sync"] = {"bound": "tensor", "achieved": tfl / (tms / 1e3) / 1e12,
+                                                "unit": "TFLOP/s", "peak": tf_peak, "ms": tms,
+                                                "kernel": "gemm_nt_kernel (mma.sync m16n8k16 BF16)"}
 
     # ---- plain single-instance GPU ADMM on a few of the same instances
     plain_n = min(args.plain, B)
@@ -677,7 +678,7 @@ def main():
     ap.add_argument("--train", type=int, default=None, help="training instances (family workload)")
     ap.add_argument("--plain", type=int, default=8, help="instances solved one at a time for the comparison")
     ap.add_argument("--cpu-instances", type=int, default=4)
-    ap.add_argument("--network-kernel", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--network-kernel", type=int, default=2, choices=[0, 1, 2],
                     help="profiling case: the network's product kernel "
                          "(0 mma.sync, 1 tcgen05 fed by cp.async, 2 tcgen05 fed by TMA)")
     ap.add_argument("--oracle-instances", type=int, default=2,

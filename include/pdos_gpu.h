@@ -216,10 +216,10 @@ int pdosgpu_mlp_time_forward(pdosgpu_mlp *p, int batch, int reps, double *ms, do
 void *pdosgpu_mlp_stream(pdosgpu_mlp *p);
 /* Waits for the network's stream; fails if a tensor-core product timed out. */
 int pdosgpu_mlp_sync(pdosgpu_mlp *p);
-/* Product kernel: 0 = mma.sync (default); 1 = tcgen05 with tensor-memory
- * accumulators, operands staged by cp.async; 2 = tcgen05, operands staged by
- * TMA (cp.async.bulk.tensor) in a producer / MMA / epilogue warp split.
- * All three give the same products. */
+/* Product kernel: 2 (default) = tcgen05 with tensor-memory accumulators,
+ * operands staged by TMA (cp.async.bulk.tensor, 128-byte swizzled tiles) in
+ * a producer / MMA / epilogue warp split; 1 = tcgen05 with operands staged
+ * by cp.async; 0 = mma.sync.  All three give the same products. */
 int pdosgpu_mlp_set_kernel(pdosgpu_mlp *p, int kind);
 void pdosgpu_mlp_free(pdosgpu_mlp *p);
 

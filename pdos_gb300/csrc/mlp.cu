@@ -397,20 +397,30 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tc_kernel(const bf16 *__rest
 // 2-D tensor maps of A and B, zero fill outside the matrices); thread 0 of
 // warp 1 waits for each full stage, issues tcgen05.mma and commits the stage
 // back to the producer; then all four warps drain tensor memory into the
-// epilogue.  A TMA box of 8 K-elements x R rows lands as R rows of 16 bytes,
-// i.e. a column of R/8 core matrices, so the no-swizzle descriptors step
-// 16 B-rows by 128 B (8-row groups) and K-chunks by the box size.
+// epilogue.  One TMA box per operand and stage, 64 K-elements (128 bytes)
+// wide, lands with the 128-byte swizzle: rows of 128 bytes whose 16-byte
+// chunks are permuted within each group of 8 rows (1,024 bytes).  The
+// shared-memory descriptors name that layout (swizzle mode 2, 1,024 bytes
+// between 8-row groups), and the four 16-deep products of a stage start 32
+// bytes apart inside the swizzled rows.  Stages are 1,024-byte aligned.
 namespace tma {
-constexpr int TM = 128, TN = 256, TK = 64, KC = TK / 8;
+constexpr int TM = 128, TN = 256, TK = 64;
 constexpr int kThreads = 128;
-constexpr int kStages = 3;
-constexpr int kAChunk = TM * 16, kBChunk = TN * 16;  // bytes of one 8-deep K chunk
-constexpr int kABytes = KC * kAChunk, kBBytes = KC * kBChunk;
-constexpr int kStageBytes = kABytes + kBBytes;        // 48 KB
+constexpr int kStages = 4;
+constexpr int kABytes = TM * 128, kBBytes = TN * 128;  // 128-byte rows of 64 K-elements
+constexpr int kStageBytes = kABytes + kBBytes;         // 48 KB
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
 constexpr uint32_t kTmemCols = TN;
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
                             ((uint32_t)(TM >> 4) << 24);
+
+// K-major operand in the 128-byte swizzled layout: start address, leading
+// byte offset 16 (unused by this layout), 1,024 bytes between 8-row groups,
+// version 1, swizzle mode 2 (128-byte).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
   asm volatile(
@@ -469,11 +479,9 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
                    "r"((uint32_t)kStageBytes)
                    : "memory");
       const uint32_t a_s = sbase + st * kStageBytes, b_s = a_s + kABytes;
-      for (int c = 0; c < KC; ++c) {
-        const int x = kt * TK + 8 * c;  // a multiple of 8 elements: 16-byte aligned
-        tma_load_2d(a_s + c * kAChunk, &tmA, x, m0, fb + 8 * st);
-        tma_load_2d(b_s + c * kBChunk, &tmB, x, n0, fb + 8 * st);
-      }
+      const int x = kt * TK;  // a multiple of 64 elements: 128-byte aligned
+      tma_load_2d(a_s, &tmA, x, m0, fb + 8 * st);
+      tma_load_2d(b_s, &tmB, x, n0, fb + 8 * st);
     }
     }
     __syncwarp();
@@ -488,9 +496,9 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a_s = sbase + st * kStageBytes, b_s = a_s + kABytes;
 #pragma unroll
-      for (int s = 0; s < TK / 16; ++s) {  // two 8-deep chunks per product
-        const uint64_t ad = tc::smem_desc(a_s + 2 * s * kAChunk, kAChunk, 128);
-        const uint64_t bd = tc::smem_desc(b_s + 2 * s * kBChunk, kBChunk, 128);
+      for (int s = 0; s < TK / 16; ++s) {  // 16 K-elements (32 bytes) per product
+        const uint64_t ad = sw128_desc(a_s + 32 * s);
+        const uint64_t bd = sw128_desc(b_s + 32 * s);
         const uint32_t acc = (kt > 0 || s > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -720,14 +728,14 @@ int Net::set_gemm(int kind) {
 }
 
 // 2-D tensor map of a row-major BF16 matrix (rows x K, leading dimension
-// ld elements, a multiple of 8): boxes of 8 K-elements x box_rows rows,
-// zero fill outside.
+// ld elements, a multiple of 8): boxes of 64 K-elements x box_rows rows
+// written with the 128-byte swizzle, zero fill outside.
 int Net::encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, int box_rows) {
   if ((reinterpret_cast<uintptr_t>(p) & 15) || (ld & 7) || K <= 0 || rows <= 0)
     return fail(PDOSGPU_EINVAL, "tensor-map operand must be 16-byte aligned with ld a multiple of 8");
   const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
-  const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+  const cuuint32_t box[2] = {(cuuint32_t)tma::TK, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1u, 1u};
   // The driver entry point is looked up through the runtime, so the library
   // itself does not link libcuda (it loads on machines without a driver).
@@ -744,7 +752,7 @@ int Net::encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, in
     encode = reinterpret_cast<EncodeTiled>(fn);
   }
   const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(p), dims, strides, box,
-                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PDOSGPU_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return PDOSGPU_OK;
@@ -776,6 +784,7 @@ int Net::create(int n_in, int hidden, int n_out, int max_batch) {
   for (int i = 0; i < 4; ++i) ld_[i] = pad8(dims_[i]);
   max_batch_ = pad8(max_batch);
   PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  PDOS_TRY(set_gemm(2));  // the TMA-fed tcgen05 products by default
   for (int l = 0; l < 3; ++l) {
     const int64_t rows = ld_[l + 1], cols = ld_[l];  // padded: zero rows / columns stay zero
     const int64_t cnt = rows * cols;

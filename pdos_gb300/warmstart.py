@@ -86,7 +86,7 @@ class Net:
         return ms.value, fl.value
 
     def set_kernel(self, kind):
-        """0: mma.sync products, 1: tcgen05 fed by cp.async, 2: tcgen05 fed by TMA."""
+        """2 (default): tcgen05 fed by TMA, 1: tcgen05 fed by cp.async, 0: mma.sync products."""
         _lib.check(self.lib.pdosgpu_mlp_set_kernel(self._p, int(kind)), "pdosgpu_mlp_set_kernel", self.lib)
         return self
 
