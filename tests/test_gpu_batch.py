@@ -70,7 +70,7 @@ def test_uneven_batch_matches_single_instance_solves(built_lib, torch_cuda):
     from pdos_gb300.solver import Batch, solve_problem
     probs = _uneven_portfolios()
     nnz = [len(p.Ax) for p in probs]
-    assert min(nnz) <= 4096 and max(nnz) > 262144  # all four size classes
+    assert min(nnz) <= 4096 and max(nnz) > 262144  # all four classes by nonzeros
     assert any(max(p.q) > 1024 for p in probs)    # CTA-wide cone path
     with Batch(probs) as b:
         outs = b.solve().fetch()
@@ -219,7 +219,7 @@ def test_autotuner_choice_is_reproducible(built_lib, torch_cuda):
     probs = _uneven_portfolios()[:6]
     with Batch(probs) as b:
         blocks = b.tune(iters=4)
-        assert all(v in (128, 256, 512) for v in blocks)
+        assert len(blocks) == 5 and all(v in (128, 256, 512, 1024) for v in blocks)
         tuned = b.solve().fetch()
     with Batch(probs) as b2:
         fixed = b2.set_blocks(blocks).solve().fetch()
