@@ -138,7 +138,11 @@ __device__ __forceinline__ T warp_sum_t(T v) {
 }
 
 // Block sums of N values; every thread adds the warp partials in the same
-// fixed order, so all threads get identical totals.  scratch: N * BLOCK/32.
+// fixed order, so all threads get identical totals.  The barrier after the
+// partials are written also orders every earlier shared-memory write.
+// Callers alternate between two scratch halves (Reduce below): the next use
+// of a half comes after another reduction's barrier, so no second barrier
+// is needed before the half is overwritten.  scratch: N * BLOCK/32.
 template <int BLOCK, int N>
 __device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
   constexpr int W = BLOCK / 32;
@@ -157,8 +161,19 @@ __device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
     for (int w = 0; w < W; ++w) t += scratch[k * W + w];
     v[k] = t;
   }
-  __syncthreads();
 }
+
+// Two scratch halves of 3 * BLOCK/32 doubles, used in turn.
+template <int BLOCK>
+struct Reduce {
+  double *scratch;
+  int half;
+  template <int N>
+  __device__ __forceinline__ void operator()(double (&v)[N]) {
+    half ^= 1;
+    block_sum_n<BLOCK, N>(v, scratch + half * 3 * (BLOCK / 32));
+  }
+};
 
 // Streaming loads of four consecutive matrix entries (16-byte aligned):
 // read-only for the kernel's lifetime and not kept in L1, which holds the
@@ -316,6 +331,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
 
   State S = *gst;  // every thread keeps its own copy of the scalars
   if (S.done) return;
+  Reduce<BLOCK> reduce{scratch, 0};
 
   // Dual update of one finished row and the next iteration's residual inputs
   // (pdos.c:232-236, linAlg.h:158-175, indirect/private.c:20-29, :58-60).
@@ -342,7 +358,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       u[r] = ((sv + lam * yv) - bv) + a;
       red[1] += (double)bv * (double)yv;
     });
-    block_sum_n<BLOCK, 2>(red, scratch);
+    reduce(red);
     S.pres_sq = red[0];
     S.by = red[1];
     S.prepped = 1;
@@ -366,7 +382,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       q[j] = qj;
       top[2] += (double)qj * (double)qj;
     });
-    block_sum_n<BLOCK, 3>(top, scratch);
+    reduce(top);
     S.p_res = sqrt(S.pres_sq);
     S.d_res = sqrt(top[0]);
     S.p_obj = top[1];
@@ -397,7 +413,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
         tt[j] = tj;
         pt[0] += (double)pj * (double)tj;
       });
-      block_sum_n<BLOCK, 1>(pt, scratch);
+      reduce(pt);
       const double step = qsold / pt[0];
       const T stp = (T)step, nstp = (T)(-step);
       double qs[1] = {0.0};
@@ -408,7 +424,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
         q[j] = qj;
         qs[0] += (double)qj * (double)qj;
       }
-      block_sum_n<BLOCK, 1>(qs, scratch);
+      reduce(qs);
       ++cg_iter;
       ++S.cg_total;
       double ratio = 0.0;
@@ -475,7 +491,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
           const T v = s[off + i];
           acc[0] += (double)(v * v);
         }
-        block_sum_n<BLOCK, 1>(acc, scratch);
+        reduce(acc);
         const T tail = (T)sqrt(acc[0]);
         for (int i = tid; i < len; i += BLOCK) {
           const int r = off + i;
@@ -483,7 +499,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
         }
       }
     }
-    block_sum_n<BLOCK, 2>(fin, scratch);
+    reduce(fin);
     S.pres_sq = fin[0];
     S.by = fin[1];
     S.admm_iter += 1;
@@ -503,7 +519,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
 template <typename T, int BLOCK, bool GLOBAL>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double scratch[3 * (BLOCK / 32)];
+  __shared__ double scratch[2 * 3 * (BLOCK / 32)];
   __shared__ Inst s_inst;
   __shared__ int s_k;
   T *g1 = staging_base<T, GLOBAL>(sm, smem_raw, B.gscratch);
