@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
   extern __shared__ unsigned char raw[];
   __shared__ uint64_t full[kStages], empty[kStages], done;
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_fail;
+  __shared__ int s_fail, s_issued;
   unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
@@ -446,6 +446,7 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
   const uint32_t db = (uint32_t)__cvta_generic_to_shared(&done);
   if (tid == 0) {
     s_fail = 0;
+    s_issued = 0;
     for (int i = 0; i < kStages; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fb + 8 * i));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(eb + 8 * i));
@@ -482,6 +483,7 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
       const int x = kt * TK;  // a multiple of 64 elements: 128-byte aligned
       tma_load_2d(a_s, &tmA, x, m0, fb + 8 * st);
       tma_load_2d(b_s, &tmB, x, n0, fb + 8 * st);
+      s_issued = kt + 1;
     }
     }
     __syncwarp();
@@ -514,8 +516,9 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
     __syncwarp();
   }
   // everyone: the last commit covers every product
-  bool ok = tc::mbar_wait_bounded(db, 0);
-  __syncthreads();
+  // one verdict for the whole CTA: the epilogue's tensor-memory loads need
+  // whole warps
+  bool ok = __syncthreads_and(tc::mbar_wait_bounded(db, 0)) != 0;
   if (s_fail) ok = false;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
@@ -539,6 +542,9 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
+    // wait (bounded) for the loads still in flight before the CTA leaves
+    for (int kt = max(0, s_issued - kStages); kt < s_issued; ++kt)
+      tc::mbar_wait_bounded(fb + 8 * (kt % kStages), (uint32_t)((kt / kStages) & 1));
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
