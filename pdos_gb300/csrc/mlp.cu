@@ -748,15 +748,16 @@ int Net::encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, in
   using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-  static EncodeTiled encode = nullptr;
-  if (!encode) {
+  static const EncodeTiled encode = []() -> EncodeTiled {  // thread-safe one-time look-up
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
-    PDOS_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
-    if (q != cudaDriverEntryPointSuccess || !fn)
-      return fail(PDOSGPU_ECUDA, "driver entry point cuTensorMapEncodeTiled not found");
-    encode = reinterpret_cast<EncodeTiled>(fn);
-  }
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<EncodeTiled>(fn);
+  }();
+  if (!encode) return fail(PDOSGPU_ECUDA, "driver entry point cuTensorMapEncodeTiled not found");
   const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(p), dims, strides, box,
                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
