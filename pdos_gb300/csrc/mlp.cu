@@ -522,7 +522,13 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
   if (s_fail) ok = false;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    const int r = m0 + warp * 32 + lane;
+    // Each warp passes its 32 x 32 accumulator blocks through a padded
+    // shared tile (the operand stages are idle now), so that the epilogue
+    // reads masks and writes outputs a row at a time with lane = column:
+    // coalesced 128-byte (FP32) or 64-byte (BF16) rows instead of 32 rows
+    // touched per store.  The arithmetic per element is store_row32's.
+    float *tile = reinterpret_cast<float *>(base) + warp * (32 * 33);
+    const int rbase = m0 + warp * 32;
 #pragma unroll 1
     for (int c0 = 0; c0 < TN; c0 += 32) {
       uint32_t v[32];
@@ -538,7 +544,27 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
             "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      tc::store_row32(ep, r, n0 + c0, M, N, v);
+      const int cb = n0 + c0;
+      if (cb >= N) continue;  // uniform over the warp
+#pragma unroll
+      for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = __uint_as_float(v[j]);
+      __syncwarp();
+      const int c = cb + lane;
+      const bool cok = c < N;
+      const float bj = (ep.bias && cok) ? __ldg(ep.bias + c) : 0.f;
+      for (int i = 0; i < 32; ++i) {
+        const int r = rbase + i;
+        if (r >= M) break;  // uniform over the warp
+        float x = tile[i * 33 + lane];
+        if (ep.bias) x += bj;
+        if (ep.relu) x = x > 0.f ? x : 0.f;
+        if (cok) {
+          if (ep.mask && !(__bfloat162float(ep.mask[(size_t)r * ep.ldm + c]) > 0.f)) x = 0.f;
+          if (ep.out_f32) ep.out_f32[(size_t)r * ep.ldc + c] = x;
+          else ep.out_bf16[(size_t)r * ep.ldc + c] = __float2bfloat16_rn(x);
+        }
+      }
+      __syncwarp();
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
