@@ -1,0 +1,230 @@
+// Host-side builder of the batch solver's hybrid matrix layout (no CUDA):
+// for every instance and each side of it (rows of A, rows of A'), slices of
+// 32 rows stored column-major and long rows cut into warp-wide pieces, with
+// instance-local 16-bit gather indices.  Used by batch.cu and tested on the
+// CPU.
+#pragma once
+
+#include <algorithm>
+#include <atomic>
+#include <cstdint>
+#include <memory>
+#include <thread>
+#include <vector>
+
+namespace pdosgpu {
+namespace batch {
+
+#ifndef PDOS_BATCH_PIECE
+#define PDOS_BATCH_PIECE 1024
+#endif
+constexpr int kLongRow = 128;               // rows with more nonzeros go to warp-wide pieces
+constexpr int kPiece = PDOS_BATCH_PIECE;    // target nonzeros per piece
+
+// One side (A: rows of A; At: rows of A', i.e. columns of A) of an instance
+// in the hybrid layout: slices of 32 consecutive rows stored column-major
+// (lane = row), and rows longer than kLongRow cut into pieces of at most
+// kPiece nonzeros, one warp per piece.
+struct Side {
+  int64_t slice0, piece0, split0;
+  int32_t nslices, npieces, nsplit, rows;
+};
+
+// Work over instances on the host's cores (atomic counter, no exceptions).
+template <class F>
+void parallel_for(int64_t n, F &&f) {
+  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(n, hw));
+  std::atomic<int64_t> next{0};
+  auto body = [&]() {
+    for (int64_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(body);
+  body();
+  for (auto &th : pool) th.join();
+}
+
+// A host array that is not zero-filled on allocation (its writers cover it).
+template <typename T>
+struct Raw {
+  std::unique_ptr<T[]> p;
+  size_t n = 0;
+  void resize(size_t count) {
+    p.reset(count ? new T[count] : nullptr);
+    n = count;
+  }
+  T *data() { return p.get(); }
+  const T *data() const { return p.get(); }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+  T &operator[](size_t i) { return p[i]; }
+  const T &operator[](size_t i) const { return p[i]; }
+  using value_type = T;
+};
+
+// Position in the layout arrays of one side.
+struct Cursor {
+  int64_t slice = 0, piece = 0, split = 0, elem = 0;
+};
+
+// The hybrid layout of one side for every instance.  walk<false> sizes an
+// instance (advances a cursor), walk<true> writes it at a cursor; both make
+// the same decisions, and every instance starts and ends on a multiple of
+// 4 elements, so instances can be sized and written in parallel.
+struct HybBuild {
+  std::vector<int64_t> slice_beg;
+  std::vector<int32_t> slice_w;
+  std::vector<uint32_t> slice_skip;
+  std::vector<int32_t> piece_row, piece_len, split_row, split_p0, split_np;
+  std::vector<int64_t> piece_beg;
+  Raw<uint16_t> idx;  // per element: local gather index
+  Raw<int32_t> src;   // per element: position of its value in the source array (-1: padding)
+
+  void resize(const Cursor &t) {
+    slice_beg.resize(t.slice);
+    slice_w.resize(t.slice);
+    slice_skip.resize(t.slice);
+    piece_row.resize(t.piece);
+    piece_len.resize(t.piece);
+    piece_beg.resize(t.piece);
+    split_row.resize(t.split);
+    split_p0.resize(t.split);
+    split_np.resize(t.split);
+    idx.resize(t.elem);
+    src.resize(t.elem);
+  }
+
+  // Rows [r0, r1) of a row-wise matrix (ptr, gidx absolute); gather indices
+  // are made local by subtracting c0.
+  template <bool WRITE, typename Idx>
+  Side walk(const int32_t *ptr, const Idx *gidx, int64_t r0, int64_t r1, int64_t c0, Cursor &c) {
+    Side sd{};
+    const int64_t R = r1 - r0;
+    sd.rows = (int32_t)R;
+    sd.slice0 = c.slice;
+    sd.piece0 = c.piece;
+    sd.split0 = c.split;
+    auto put = [&](int32_t j, int32_t p) {
+      if (WRITE) {
+        idx[c.elem] = (uint16_t)j;
+        src[c.elem] = p;
+      }
+      ++c.elem;
+    };
+    auto pad4 = [&]() {
+      while (c.elem % 4) put(0, -1);  // zero entries up to 16-byte alignment
+    };
+    for (int64_t s0 = 0; s0 < R; s0 += 32) {
+      uint32_t skip = 0;
+      int width = 0;
+      for (int lane = 0; lane < 32; ++lane) {
+        const int64_t r = s0 + lane;
+        if (r >= R) {
+          skip |= 1u << lane;
+          continue;
+        }
+        const int len = ptr[r0 + r + 1] - ptr[r0 + r];
+        if (len > kLongRow) {
+          skip |= 1u << lane;
+          continue;
+        }
+        width = std::max(width, len);
+      }
+      const bool vec = width >= 4;
+      if (vec) {
+        width = (width + 3) & ~3;
+        pad4();
+      }
+      if (WRITE) {
+        slice_beg[c.slice] = c.elem;
+        slice_w[c.slice] = vec ? -width : width;
+        slice_skip[c.slice] = skip;
+      }
+      for (int cidx = 0; cidx < width; cidx += vec ? 4 : 1) {
+        for (int lane = 0; lane < 32; ++lane) {
+          for (int t = 0; t < (vec ? 4 : 1); ++t) {
+            const int64_t r = s0 + lane;
+            int32_t j = 0, p = -1;
+            if (!((skip >> lane) & 1u)) {
+              const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
+              if (cidx + t < len) {
+                p = (int32_t)(a + cidx + t);
+                j = (int32_t)(gidx[a + cidx + t] - c0);
+              }
+            }
+            put(j, p);
+          }
+        }
+      }
+      ++c.slice;
+      ++sd.nslices;
+    }
+    for (int64_t r = 0; r < R; ++r) {
+      const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
+      if (len <= kLongRow) continue;
+      const int64_t np = (len + kPiece - 1) / kPiece;
+      if (np > 1) {
+        if (WRITE) {
+          split_row[c.split] = (int32_t)r;
+          split_p0[c.split] = (int32_t)(c.piece - sd.piece0);
+          split_np[c.split] = (int32_t)np;
+        }
+        ++c.split;
+        ++sd.nsplit;
+      }
+      for (int64_t k = 0; k < np; ++k) {  // nearly equal pieces
+        const int64_t e0 = a + len * k / np, e1 = a + len * (k + 1) / np;
+        pad4();
+        const int64_t beg = c.elem;
+        for (int64_t e = e0; e < e1; ++e) put((int32_t)(gidx[e] - c0), (int32_t)e);
+        pad4();
+        if (WRITE) {
+          piece_row[c.piece] = np > 1 ? ~(int32_t)r : (int32_t)r;
+          piece_beg[c.piece] = beg;
+          piece_len[c.piece] = (int32_t)(c.elem - beg);
+        }
+        ++c.piece;
+        ++sd.npieces;
+      }
+    }
+    pad4();
+    return sd;
+  }
+};
+
+// Sizes every instance, turns the sizes into start cursors, then writes the
+// instances in parallel; side(i) returns (ptr, gidx, r0, r1, c0) of one.
+template <typename Idx, class SideOf>
+void build_layout(HybBuild &hb, int64_t count, SideOf side, std::vector<Side> &out) {
+  std::vector<Cursor> size(count);
+  parallel_for(count, [&](int64_t i) {
+    const int32_t *ptr;
+    const Idx *gidx;
+    int64_t r0, r1, c0;
+    side(i, ptr, gidx, r0, r1, c0);
+    Cursor c;
+    hb.walk<false>(ptr, gidx, r0, r1, c0, c);
+    size[i] = c;
+  });
+  std::vector<Cursor> start(count + 1);
+  for (int64_t i = 0; i < count; ++i) {
+    start[i + 1].slice = start[i].slice + size[i].slice;
+    start[i + 1].piece = start[i].piece + size[i].piece;
+    start[i + 1].split = start[i].split + size[i].split;
+    start[i + 1].elem = start[i].elem + size[i].elem;
+  }
+  hb.resize(start[count]);
+  out.assign(count, Side{});
+  parallel_for(count, [&](int64_t i) {
+    const int32_t *ptr;
+    const Idx *gidx;
+    int64_t r0, r1, c0;
+    side(i, ptr, gidx, r0, r1, c0);
+    Cursor c = start[i];
+    out[i] = hb.walk<true>(ptr, gidx, r0, r1, c0, c);
+  });
+}
+
+}  // namespace batch
+}  // namespace pdosgpu
