@@ -56,6 +56,49 @@ def _c_problem(prob, keep):
         float(p["CG_TOL"]), int(p["VERBOSE"]), int(p["NORMALIZE"]))
 
 
+_F64, _I64 = np.dtype(np.float64), np.dtype(np.int64)
+
+
+def _addr(a, dt, keep):
+    """Address of `a` as a contiguous array of dtype dt (a copy goes to keep); 0 for None."""
+    if a is None:
+        return 0
+    if not (type(a) is np.ndarray and a.dtype == dt and a.flags.c_contiguous):
+        a = np.ascontiguousarray(a, dt)
+    keep.append(a)
+    return a.ctypes.data
+
+
+def _c_problems(probs, keep):
+    """ctypes array of pdosgpu_problem for many Problems, the same bytes as
+    _c_problem one by one: the 21 eight-byte fields of every problem are
+    gathered column by column into one numpy buffer (kept in keep), which
+    the array views without a copy."""
+    n = len(probs)
+    cols = [[] for _ in range(21)]
+    for p in probs:
+        par = p.params
+        q = np.asarray(p.q, np.int64) if len(p.q) else np.zeros(1, np.int64)
+        vals = (p.n, p.m, _addr(p.Ax, _F64, keep), _addr(p.Ai, _I64, keep), _addr(p.Ap, _I64, keep),
+                _addr(p.b, _F64, keep), _addr(p.c, _F64, keep), _addr(p.x0, _F64, keep),
+                _addr(p.y0, _F64, keep), _addr(p.s0, _F64, keep), p.f, p.l, len(p.q), _addr(q, _I64, keep),
+                int(par["MAX_ITERS"]), int(par["CG_MAX_ITS"]), float(par["EPS_ABS"]), float(par["ALPHA"]),
+                float(par["CG_TOL"]), int(par["VERBOSE"]), int(par["NORMALIZE"]))
+        for k, v in enumerate(vals):
+            cols[k].append(v)
+    assert ctypes.sizeof(_lib.Problem) == 21 * 8
+    buf = np.empty((max(n, 1), 21), np.int64)
+    fbuf = buf.view(np.float64)
+    if n:
+        for k in range(21):
+            if k in (16, 17, 18):  # eps_abs, alpha, cg_tol
+                fbuf[:, k] = np.asarray(cols[k], np.float64)
+            else:
+                buf[:, k] = np.asarray(cols[k], np.int64)
+    keep.append(buf)
+    return (_lib.Problem * n).from_buffer(buf)
+
+
 class Workspace:
     """A problem resident on the GPU (pdosgpu_setup ... pdosgpu_free)."""
 
@@ -134,7 +177,7 @@ class Batch:
         self.lib = _lib.load()
         self.probs = list(probs)
         self._keep = []
-        arr = (_lib.Problem * len(self.probs))(*[_c_problem(p, self._keep) for p in self.probs])
+        arr = _c_problems(self.probs, self._keep)
         self._keep.append(arr)
         self._opt = make_options(precision, "2norm", device)
         self._b = ctypes.c_void_p()

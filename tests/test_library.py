@@ -99,3 +99,21 @@ def test_no_gpu_fails_loudly(built_lib):
         Workspace(prob)
     with pytest.raises(RuntimeError, match="NULL"):
         pdos_call(prob)
+
+
+def test_batch_marshalling_matches_one_by_one():
+    """Batch's vectorised pdosgpu_problem array has the bytes of the
+    per-problem marshalling (same fields, same array addresses)."""
+    import numpy as np
+    from pdos_gb300 import generators as g
+    from pdos_gb300.solver import _c_problem, _c_problems
+    probs = [g.portfolio(30, 3, 0.5, seed=1, params=dict(EPS_ABS=1e-3, VERBOSE=0)),
+             g.portfolio(50, 5, 0.5, seed=2, params=dict(ALPHA=1.6, CG_MAX_ITS=7, NORMALIZE=1)),
+             g.random_feasible(m=40, n=12, nnz_per_col=3, seed=3, params=dict(MAX_ITERS=77))]
+    probs[1] = probs[1].with_warm_start(x0=np.ones(probs[1].n), s0=np.zeros(probs[1].m))
+    keep_a, keep_b = [], []
+    a = _c_problems(probs, keep_a)
+    b = [_c_problem(p, keep_b) for p in probs]
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert bytes(x) == bytes(y)
