@@ -51,3 +51,40 @@ def test_fixture_goldens_present():
     names = solve_cases()
     assert sum(n.startswith("fixture") for n in names) == 10
     assert len(names) >= 30
+
+
+def _cone_blocks(f, l, q):
+    """Index ranges of the zero, orthant and SOC blocks."""
+    out, off = [], f + l
+    for k in q:
+        out.append((off, off + k))
+        off += k
+    return out
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_port_projection_properties(port, seed):
+    """The oracle's cone projection is a projection: its output lies in the
+    cone, projecting twice changes nothing, and on the self-dual blocks
+    (orthant, second-order cones) v = P(v) - P(-v) with P(v) orthogonal to
+    P(v) - v (Moreau's decomposition)."""
+    rng = np.random.default_rng(seed)
+    f, l = int(rng.integers(0, 5)), int(rng.integers(0, 9))
+    q = [int(k) for k in rng.integers(1, 40, size=int(rng.integers(1, 6)))] + [1, 2]
+    m = f + l + sum(q)
+    v = rng.standard_normal(m) * rng.choice([1e-3, 1.0, 1e3])
+    p = port.proj_cone_q(v, f, l, np.array(q))
+    scale = 1.0 + np.abs(v).max()
+    tol = 1e-12 * scale
+    # membership
+    assert np.all(p[:f] == 0.0)
+    assert np.all(p[f:f + l] >= 0.0)
+    for a, b in _cone_blocks(f, l, q):
+        assert p[a] >= np.linalg.norm(p[a + 1:b]) - tol
+    # idempotence
+    np.testing.assert_allclose(port.proj_cone_q(p, f, l, np.array(q)), p, rtol=0, atol=tol)
+    # Moreau on the self-dual part
+    pn = port.proj_cone_q(-v, f, l, np.array(q))
+    np.testing.assert_allclose((p - pn)[f:], v[f:], rtol=0, atol=tol)
+    for a, b in [(f, f + l)] + _cone_blocks(f, l, q):
+        assert abs(np.dot(p[a:b], p[a:b] - v[a:b])) <= 1e-10 * scale * scale
