@@ -27,7 +27,9 @@ JSON line (rank 0):
            solve's device time): algorithmic bytes of the products it ran
            (values and indices of A and A', pointers, gathered and written
            vectors) / its device time, against the measured HBM copy peak;
-           the CG products alone are timed beside it (spmv_products)
+           the CG products alone are timed beside it (spmv_products), and
+           the network's forward pass against the measured BF16 peak
+           (network_forward: TMA-fed tcgen05 kernel; mma.sync beside it)
   cpu_baseline  the oracle (C restatement of the reference, 1 core) solving
            a few held-out instances from the cold start
 --impl reference runs that CPU solver on all host cores instead.
