@@ -262,16 +262,23 @@ int pdosgpu_proj_cone_f64(double *v, int64_t f, int64_t l, int64_t qsize,
  * allocate device memory while they run (memory owned by a pool allocator
  * that must not be bypassed, regions where allocation is forbidden or would
  * synchronise the device).  It calls no cudaMalloc/cudaFree: its scratch is a
- * static device array of about 3 MB built into the library, held by every
- * GPU that loads the library until the process exits.  Limits: at most 65,536
- * second-order cones and 131,072 chunks of 4,096 rows (sum over cones of
+ * static device array of about 3 MB built into the library.  With CUDA's
+ * lazy module loading (the default) the driver places that array, and the
+ * projection's kernels, in a context the first time they are used there, and
+ * keeps them until the context is destroyed: so the first call in a context
+ * is the one that allocates.  Make one warm-up call per device (or context),
+ * projecting at least one second-order cone and one zero or nonnegative row,
+ * before any region that must not allocate and before any stream capture.
+ * The scratch address is looked up once per context (cudaGetSymbolAddress)
+ * and cached by the context's unique id, so a context re-created after
+ * cudaDeviceReset gets a fresh look-up.  Limits: at most 65,536 second-order
+ * cones and 131,072 chunks of 4,096 rows (sum over cones of
  * ceil(q[i]/4096)); larger requests return PDOSGPU_EINVAL without touching
- * the GPU.  The first call on a device looks the array's address up
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls share the array, so calls whose work
- * overlaps on the GPU race; serialise them on one stream.  q is a HOST
- * array; the call returns once the work is queued on `stream`.  This entry
- * point has no counterpart in the reference. */
+ * the GPU.  All calls share the array, so calls whose work overlaps on the
+ * GPU race; serialise them on one stream.  q is a HOST array, copied with
+ * cudaMemcpyAsync (a pageable q is staged before the call returns, so q may
+ * be reused at once); the call returns once the work is queued on `stream`.
+ * This entry point has no counterpart in the reference. */
 int pdosgpu_proj_cone_f64_noalloc(double *v, int64_t f, int64_t l, int64_t qsize,
                                   const int64_t *q, void *stream);
 

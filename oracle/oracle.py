@@ -28,7 +28,7 @@ REF_SO = {
     "direct": os.path.join(HERE, "_ref", "libpdosdir_ref.so"),
     "ruiz": os.path.join(HERE, "_ref", "libpdosindir_ruiz_ref.so"),
 }
-REF_SRC = os.environ.get("PDOS_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.environ.get("PDOS_REFERENCE_DIR", "")  # the reference's source tree, if any
 
 _D = POINTER(c_double)
 _I = POINTER(c_int64)
@@ -40,11 +40,13 @@ def build_port(force=False):
     return PORT_SO
 
 
-def build_ref():
-    """Compile the reference from its sources (only where they exist)."""
-    if not os.path.isdir(REF_SRC):
+def build_ref(src=None):
+    """Compile the reference from its sources (only where they exist): `src`
+    or the directory named by PDOS_REFERENCE_DIR."""
+    src = src or REF_SRC
+    if not src or not os.path.isdir(src):
         return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
     return True
 
 

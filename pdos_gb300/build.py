@@ -9,7 +9,10 @@ links two shared libraries into pdos_gb300/lib:
 * libpdosindir_i32.so  idxint = int
 
 Both carry the same kernels and C-ABI layer; they differ only in the
-pdos()/freeData()/freeSol() struct layout.
+pdos()/freeData()/freeSol() struct layout.  The demo command-line solvers
+(demo_indirect, demo_indirect_i32: csrc/demo_indirect.c) are then compiled
+as plain C against include/pdos.h and linked with -lpdosindir, the way a C
+caller of the reference's library builds.
 """
 import os
 import subprocess
@@ -22,6 +25,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "lib")
 OBJ = os.path.join(LIB, "obj")
 NVCC = os.environ.get("NVCC", "nvcc")
+CC = os.environ.get("CC", "gcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                 "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
@@ -40,6 +44,11 @@ TARGETS = {
     "libpdosindir.so": ["engine.o", "api.o", "batch.o", "mlp.o", "noalloc.o", "abi_l.o"],
     "libpdosindir_i32.so": ["engine.o", "api.o", "batch.o", "mlp.o", "noalloc.o", "abi_i.o"],
 }
+# C programs linked against the libraries: (executable, library, C flags)
+PROGRAMS = [
+    ("demo_indirect", "pdosindir", ["-DDLONG"]),
+    ("demo_indirect_i32", "pdosindir_i32", []),
+]
 
 
 def _sources_mtime():
@@ -71,7 +80,7 @@ def build(force=False, verbose=False):
     present = {u[0] for u in units}
     newest = _sources_mtime()
     up_to_date = all(os.path.exists(lib_path(t)) and os.path.getmtime(lib_path(t)) >= newest
-                     for t in TARGETS)
+                     for t in list(TARGETS) + [p[0] for p in PROGRAMS])
     if up_to_date and not force:
         return lib_path()
     with ThreadPoolExecutor(max_workers=min(len(units), os.cpu_count() or 4)) as ex:
@@ -84,6 +93,15 @@ def build(force=False, verbose=False):
             raise RuntimeError(f"link of {target} failed:\n{r.stderr}")
         if verbose:
             print("built", lib_path(target))
+    for exe, lib, cflags in PROGRAMS:
+        cmd = [CC, "-O2", "-std=c99", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include")] + cflags + \
+              [os.path.join(CSRC, "demo_indirect.c"), "-L", LIB, "-l" + lib, "-Wl,-rpath,$ORIGIN",
+               "-o", lib_path(exe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of {exe} failed:\n{r.stderr}")
+        if verbose:
+            print("built", lib_path(exe))
     return lib_path()
 
 

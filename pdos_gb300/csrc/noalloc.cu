@@ -10,12 +10,20 @@
 // cone offsets, per-chunk partial norms and cone heads -- in a fixed-size
 // static device array instead of allocating it.
 //
-// The array below is part of the library image: every GPU that loads the
-// library holds it (about 3 MB) until the process exits.  All calls share it
-// and it keeps the last call's contents; every slot a call reads is written
-// earlier in the same call, so nothing has to start at zero.  Calls whose
-// kernels overlap on the GPU (different streams, or different host threads
-// on the same stream ordering) race on the array.
+// The array below belongs to this file's module.  With CUDA's lazy module
+// loading (the default), the driver loads the module, the array (about
+// 3 MB) and each kernel into a context when they are first used there, and
+// that memory stays until the context is destroyed.  So the first call in a
+// context is the one that allocates: make one call per device (or per
+// context) that projects at least one second-order cone and one zero or
+// nonnegative row, so that every kernel of the projection has run, before
+// any region that must not allocate and before any stream capture.  All
+// calls share the array and it keeps the last call's contents; every slot a
+// call reads is written earlier in the same call, so nothing has to start at
+// zero.  Calls whose kernels overlap on the GPU (different streams, or
+// different host threads on the same stream ordering) race on the array.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "admm_ops.cuh"
@@ -29,7 +37,7 @@ constexpr int kNaMaxChunks = 1 << 17;  // 4096-row chunks over all cones per cal
 constexpr int kNaChunk = 4096;         // rows per chunk
 constexpr int kNaBlock = 256;
 constexpr int kNaScan = 1024;
-constexpr int kNaMaxDevices = 64;
+constexpr int kNaMaxContexts = 64;
 
 // layout of the static scratch (byte offsets)
 constexpr size_t kNaQ = 0;                                         // int64 q[kNaMaxCones]
@@ -172,25 +180,78 @@ __global__ void __launch_bounds__(kNaBlock) na_apply_kernel(NaView s, int ncones
   for (long long r = r0 + threadIdx.x; r < r1; r += kNaBlock) v[r] = soc_apply(v[r], r == head, hv, tail);
 }
 
-std::mutex g_na_mutex;
-void *g_na_ptr[kNaMaxDevices] = {};
-
-// Device address of the static scratch on the current device.  The first
-// call on a device looks it up (cudaGetSymbolAddress) with that device
-// current; later calls reuse it.
-int na_scratch(unsigned char **out) {
-  int dev = 0;
-  PDOS_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNaMaxDevices) return fail(PDOSGPU_ENOTSUP, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_ptr[dev]) {
+// Unique id of the calling thread's current context (cuCtxGetId: never
+// reused within a process), or 0 when no context is current yet.  The
+// driver functions are looked up through the runtime, so the library does
+// not link libcuda.
+int current_context_id(unsigned long long *id) {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  struct Fns {
+    GetCurrent current = nullptr;
+    GetId get_id = nullptr;
+  };
+  static const Fns fns = []() {  // thread-safe one-time look-up
+    Fns f;
     void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(PDOSGPU_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_na_ptr[dev] = p;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      f.current = reinterpret_cast<GetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      f.get_id = reinterpret_cast<GetId>(p);
+    return f;
+  }();
+  if (!fns.current || !fns.get_id) return fail(PDOSGPU_ECUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId not found");
+  CUcontext ctx = nullptr;
+  if (fns.current(&ctx) != CUDA_SUCCESS) return fail(PDOSGPU_ECUDA, "cuCtxGetCurrent failed");
+  *id = 0;
+  if (ctx && fns.get_id(ctx, id) != CUDA_SUCCESS) return fail(PDOSGPU_ECUDA, "cuCtxGetId failed");
+  return PDOSGPU_OK;
+}
+
+std::mutex g_na_mutex;
+unsigned long long g_na_ctx[kNaMaxContexts] = {};  // context ids, 0 = free slot
+void *g_na_ptr[kNaMaxContexts] = {};
+int g_na_next = 0;  // slot to reuse once all are taken
+
+// Device address of the static scratch in the current context.  The first
+// call in a context looks it up (cudaGetSymbolAddress, which loads this
+// module into the context if it is not loaded yet); later calls reuse it.
+// The cache is keyed by the context's unique id, so a context destroyed and
+// created again (cudaDeviceReset) gets a fresh look-up, never a stale
+// address.
+int na_scratch(unsigned char **out) {
+  unsigned long long id = 0;
+  PDOS_TRY(current_context_id(&id));
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (id != 0) {
+    for (int i = 0; i < kNaMaxContexts; ++i) {
+      if (g_na_ctx[i] == id) {
+        *out = static_cast<unsigned char *>(g_na_ptr[i]);
+        return PDOSGPU_OK;
+      }
+    }
   }
-  *out = static_cast<unsigned char *>(g_na_ptr[dev]);
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(PDOSGPU_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  if (id == 0) PDOS_TRY(current_context_id(&id));  // the look-up made the primary context current
+  if (id != 0) {
+    int slot = -1;
+    for (int i = 0; i < kNaMaxContexts && slot < 0; ++i)
+      if (g_na_ctx[i] == 0) slot = i;
+    if (slot < 0) {
+      slot = g_na_next;
+      g_na_next = (g_na_next + 1) % kNaMaxContexts;
+    }
+    g_na_ctx[slot] = id;
+    g_na_ptr[slot] = p;
+  }
+  *out = static_cast<unsigned char *>(p);
   return PDOSGPU_OK;
 }
 
@@ -213,17 +274,21 @@ extern "C" int pdosgpu_proj_cone_f64_noalloc(double *v, int64_t f, int64_t l, in
   if (nchunks > kNaMaxChunks)
     return fail(PDOSGPU_EINVAL,
                 "pdosgpu_proj_cone_f64_noalloc: cones need more than 131072 chunks of 4096 rows");
+  // the scratch address in this context (looked up by the first call made
+  // in the context)
+  unsigned char *base = nullptr;
+  PDOS_TRY(na_scratch(&base));
   if (m == 0) return PDOSGPU_OK;
   if (!v) return fail(PDOSGPU_EINVAL, "NULL vector");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  unsigned char *base = nullptr;
-  PDOS_TRY(na_scratch(&base));
   const NaView s = na_view(base);
   if (f + l > 0) {
     const int g = (int)std::min<int64_t>((f + l + 255) / 256, 4096);
     proj_lin_kernel<double><<<g, 256, 0, st>>>(v, f, l);
   }
   if (qsize > 0) {
+    // q is host memory: a pageable q is staged by the driver before this
+    // copy returns, so the caller may reuse q at once
     PDOS_CUDA_TRY(cudaMemcpyAsync(s.q, q, sizeof(int64_t) * qsize, cudaMemcpyHostToDevice, st));
     na_scan_kernel<<<1, kNaScan, 0, st>>>(s, (int)qsize, (long long)(f + l));
     na_chunk_sq_kernel<<<(int)nchunks, kNaBlock, 0, st>>>(s, (int)qsize, v);

@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run in a checkout where the reference's sources exist (default
-/root/reference, override with PDOS_REFERENCE_DIR):
+Run in a checkout where the reference's sources exist, naming their
+directory:
 
-    python tests/golden/make_golden.py
+    PDOS_REFERENCE_DIR=<reference source tree> python tests/golden/make_golden.py
 
 It compiles the reference with ``make -C oracle ref`` and records, for every
 case, the inputs and the reference's own outputs: x, s, y, status and the

@@ -60,6 +60,24 @@ def test_noalloc_projection_matches_allocating_entry_point(built_lib, torch_cuda
         assert np.array_equal(got == 0, want == 0)
 
 
+def test_noalloc_call_leaves_free_device_memory_unchanged(built_lib, torch_cuda):
+    """After one warm-up call (which may load the module and its static
+    array), a second call must not change the device's free memory."""
+    torch = torch_cuda
+    f, l, q = 3, 9, [200000, 5000, 4, 70000]
+    v = _vector(np.random.default_rng(7), f, l, q)
+    dv = torch.as_tensor(v, dtype=torch.float64, device="cuda")
+    qa = np.ascontiguousarray(q, np.int64)
+    qp = qa.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    assert built_lib.pdosgpu_proj_cone_f64_noalloc(dv.data_ptr(), f, l, len(q), qp, None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert built_lib.pdosgpu_proj_cone_f64_noalloc(dv.data_ptr(), f, l, len(q), qp, None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_noalloc_rejects_requests_beyond_its_scratch(built_lib, torch_cuda):
     q = np.ones(70000, np.int64)  # more cones than the static scratch holds
     v = torch_cuda.zeros(len(q), dtype=torch_cuda.float64, device="cuda")
@@ -67,3 +85,10 @@ def test_noalloc_rejects_requests_beyond_its_scratch(built_lib, torch_cuda):
         v.data_ptr(), 0, 0, len(q), q.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None)
     assert rc != 0
     assert "65536" in built_lib.pdos_gpu_last_error().decode()
+    # fewer cones, but more 4096-row chunks than the scratch holds: rejected
+    # on the host before any device work, so a small vector stands in
+    q = np.full(40000, 16385, np.int64)  # 5 chunks each
+    rc = built_lib.pdosgpu_proj_cone_f64_noalloc(
+        v.data_ptr(), 0, 0, len(q), q.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None)
+    assert rc != 0
+    assert "131072" in built_lib.pdos_gpu_last_error().decode()
