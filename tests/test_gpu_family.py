@@ -1,0 +1,90 @@
+"""Parity on the benchmarked family itself: factor-model portfolios with
+n = 2,000 assets, k = 200 factors and F at 20 % shared by the family
+(N = 2,201 variables, m = 4,402 rows, 86,402 nonzeros per instance), solved
+by the FP32 batch (FP64 reductions) at EPS_ABS 1e-4 from the cold start and
+from the learned warm start.
+
+The bar is the one the bench's headline is held to: every objective within
+1e-3 relative of the FP64 oracle, i.e. the reference's indirect algorithm
+(the C restatement, pinned bit for bit to the compiled reference) solved to
+EPS_ABS 1e-8 with CG_MAX_ITS 200 and CG_TOL 1e-12.  Those oracle solutions
+are committed (tests/golden/family_n2000_oracle.npz, made by
+tests/golden/make_family_golden.py) for 16 instances spread over the
+bench's 4,096-instance held-out draw; the test first proves it regenerated
+the same instances from their fingerprints.
+"""
+import numpy as np
+import pytest
+
+from golden_util import load_npz
+
+pytestmark = pytest.mark.gpu
+
+OBJ_TOL = 1e-3  # relative objective error against the FP64 oracle
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def family_case():
+    import sys
+    import os
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_family_golden as G
+    z = load_npz("family_n2000_oracle.npz")
+    idx = z["indices"]
+    probs = G.instances(idx)
+    for p, fp in zip(probs, z["fingerprints"]):
+        np.testing.assert_allclose(G.fingerprint(p), fp, rtol=1e-13)
+    from pdos_gb300.generators import PortfolioFamily
+    fam = PortfolioFamily(**G.FAMILY)
+    mus, ds = fam.draw(G.DRAW_COUNT, seed=G.DRAW_SEED)
+    return {"probs": probs, "objective": z["objective"], "fam": fam, "mus": mus[idx], "ds": ds[idx],
+            "params": G.PARAMS}
+
+
+def _objective_errors(probs, outs, want):
+    got = np.array([float(p.c @ o["x"]) for p, o in zip(probs, outs)])
+    return np.abs(got - want) / np.maximum(1.0, np.abs(want))
+
+
+def test_family_batch_cold_start_matches_fp64_oracle(built_lib, torch_cuda, family_case):
+    from pdos_gb300.solver import Batch
+    probs = family_case["probs"]
+    with Batch(probs, precision="fp32") as b:
+        outs = b.solve().fetch()
+    assert all(o["status"] == "Solved" for o in outs)
+    err = _objective_errors(probs, outs, family_case["objective"])
+    assert err.max() <= OBJ_TOL, err
+
+
+def test_family_batch_warm_start_matches_fp64_oracle(built_lib, torch_cuda, family_case):
+    """A network trained here on GPU solutions of 1,024 other instances of the
+    family gives the starting points; the solver's results, not the
+    network's, must meet the same bar as the cold start, in fewer ADMM
+    iterations on average."""
+    from pdos_gb300.solver import Batch
+    from pdos_gb300.warmstart import FamilyWarmStart, solve_family
+    fam, params = family_case["fam"], family_case["params"]
+    tmus, tds = fam.draw(1024, seed=11)
+    X, Y, S, _ = solve_family(fam, tmus, tds, dict(params, EPS_ABS=1e-5), "fp32")
+    ws = FamilyWarmStart(fam, hidden=256, max_batch=len(family_case["probs"]), seed=0)
+    try:
+        ws.fit(tmus, tds, X, Y, S, epochs=20, batch=128, lr=1e-3)
+        probs = family_case["probs"]
+        with Batch(probs, precision="fp32") as b:
+            cold = b.solve().fetch()
+            warm, stats = ws.solve(b, family_case["mus"], family_case["ds"], fallback_params=params)
+    finally:
+        ws.net.close()
+    assert stats["fallbacks"] == 0
+    assert all(o["status"] == "Solved" for o in warm)
+    err = _objective_errors(probs, warm, family_case["objective"])
+    assert err.max() <= OBJ_TOL, err
+    assert np.mean([o["iters"] for o in warm]) < np.mean([o["iters"] for o in cold])

@@ -40,3 +40,22 @@ def test_random_feasible_optimality():
     p = random_feasible(600, 200, 20, seed=1)
     p.check()
     assert p.f == 60 and p.l == 240 and p.q.min() >= 3
+
+
+def test_family_oracle_fixture_is_consistent():
+    """The committed FP64-oracle solutions of the benchmarked family belong to
+    the instances the generator makes today, are feasible, and their
+    objective is c'x."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_family_golden as G
+    from golden_util import load_npz
+    z = load_npz("family_n2000_oracle.npz")
+    probs = G.instances(z["indices"])
+    n = G.FAMILY["n"]
+    for p, fp, x, obj in zip(probs, z["fingerprints"], z["x"], z["objective"]):
+        np.testing.assert_allclose(G.fingerprint(p), fp, rtol=1e-13)
+        assert abs(float(p.c @ x) - obj) <= 1e-12 * max(1.0, abs(obj))
+        assert abs(x[:n].sum() - 1.0) < 1e-6 and x[:n].min() > -1e-6
+    assert (z["iters"] > 0).all() and z["tight"][0] == 1e-8
