@@ -87,6 +87,11 @@ BATCH_WORKLOADS = {
     # uneven instances: n ~ U[50, 2000], k = ceil(n/10), F at 20 %
     "portfolio_mix_batch": dict(kind="mix", batch=4096, n_lo=50, n_hi=2000, density=0.2, seed=2,
                                 precision="fp32", params=_BATCH_PARAMS),
+    # the uneven batch at its full size: 4,096 instances with n ~ U[50, 20,000]
+    # (about 1.1e10 nonzeros), generated on the host cores and set up on the
+    # device in waves of 256 instances, never all on the host at once
+    "portfolio_uneven_full": dict(kind="mix_waves", batch=4096, n_lo=50, n_hi=20000, density=0.2, seed=3,
+                                  precision="fp32", params=_BATCH_PARAMS, wave=256),
 }
 DEFAULT_WORKLOAD = "portfolio_family_warmstart"
 
@@ -482,6 +487,191 @@ def run_batch_reference(args, wl):
     return 0
 
 
+def _gen_mix_instance(job):
+    n, k, density, seed, params = job
+    from pdos_gb300 import generators as g
+    return g.portfolio(n, k, density, seed=seed, params=params)
+
+
+def _cpu_iter_sample(job):
+    prob, iters = job
+    return cpu_sample(prob, iters)
+
+
+def _portfolio_shape(n, k, density):
+    """(N, m, nnz) of a portfolio instance (pdos_gb300.generators.portfolio)."""
+    per_row = min(max(int(round(density * k)), 0), k)
+    return n + k + 1, 2 * n + 2 * k + 2, n * (3 + per_row) + 2 * k + 1
+
+
+def run_batch_waves(args, wl):
+    """The uneven batch at full size (about 1.1e10 nonzeros): instances are
+    generated in a spawn pool on the host cores, one wave ahead of the wave
+    being appended (pdosgpu_batch_append), so that at most two waves of
+    problem data exist on the host; one cold-start solve is timed (a solve
+    takes minutes, so the step count is 1).  The CPU baseline and the FP64
+    checks run on one sampled instance per n-decile."""
+    import multiprocessing as mp
+    import torch
+    from pdos_gb300 import build, generators as g
+    build.build()
+    from pdos_gb300.solver import Batch, Workspace
+    ws_n, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    count = args.batch or wl["batch"]
+    prec = wl["precision"]
+    sv = 8 if prec == "fp64" else 4
+    sizes = g.portfolio_batch_sizes(count, wl["n_lo"], wl["n_hi"], seed=wl["seed"])
+    seed0 = wl["seed"] * 1_000_003
+    jobs = [(n, k, wl["density"], seed0 + i, wl["params"]) for i, (n, k) in enumerate(sizes)]
+    shapes = [_portfolio_shape(n, k, wl["density"]) for n, k in sizes]
+    ns = np.array([n for n, _ in sizes])
+    edges = np.quantile(ns, np.linspace(0, 1, 11))
+    decile = np.clip(np.searchsorted(edges, ns, side="right") - 1, 0, 9)
+    samples = {int(np.nonzero(decile == d)[0][0]): d for d in range(10) if (decile == d).any()}
+    kept = {}
+    cores = os.cpu_count() or 2
+    pool = mp.get_context("spawn").Pool(max(1, cores - 1))
+    W = wl["wave"]
+    wave_idx = [list(range(w, min(count, w + W))) for w in range(0, count, W)]
+    t_gen = [0.0]
+
+    def waves():
+        pending = pool.map_async(_gen_mix_instance, [jobs[i] for i in wave_idx[0]], chunksize=1)
+        for w, idx in enumerate(wave_idx):
+            t0 = time.perf_counter()
+            probs = pending.get()
+            t_gen[0] += time.perf_counter() - t0
+            if w + 1 < len(wave_idx):
+                pending = pool.map_async(_gen_mix_instance, [jobs[i] for i in wave_idx[w + 1]], chunksize=1)
+            for i, p in zip(idx, probs):
+                if i in samples:
+                    kept[i] = p
+            yield probs
+            del probs
+
+    t0 = time.perf_counter()
+    batch = Batch.in_waves(waves(), precision=prec, device=local)
+    t_setup_wall = time.perf_counter() - t0
+    blocks = batch.tune(2)
+    stream = torch.cuda.ExternalStream(batch.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    batch.reset()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        batch.solve()
+        ev1.record(stream)
+        ev1.synchronize()
+    solve_ms = ev0.elapsed_time(ev1)
+    t0 = time.perf_counter()
+    x, s_, y, inf = batch.fetch_all()
+    t_fetch = time.perf_counter() - t0
+    launches = inf[0]["kernel_launches"]
+    value = count / (solve_ms / 1e3)
+
+    class _Shape:
+        def __init__(self, N, m, nnz):
+            self.n, self.m, self.nnz = N, m, nnz
+    shp = [_Shape(*sh) for sh in shapes]
+    roof_bytes = product_bytes(shp, inf, sv)
+    peak, peak_kind = measured_peaks()
+    pm, pb = batch.time_products(1)
+    achieved = roof_bytes / (solve_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "batch_admm_kernel (whole fused ADMM iteration per CTA)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind, "traffic": batch_traffic("portfolio_family_warmstart", roof_bytes),
+                "algorithmic_bytes_of_solve": roof_bytes, "ms_of_solve": solve_ms,
+                "spmv_products": {"kernel": "batch_products_kernel (u = A p, t = p + A'u)",
+                                  "achieved": pb / (pm / 1e3) / 1e9, "ms": pm, "bytes": pb,
+                                  "frac": pb / (pm / 1e3) / 1e9 / peak}}
+    cls = batch.classes()
+    iters = np.array([d["admm_iters"] for d in inf])
+    starts_x = np.concatenate([[0], np.cumsum([sh[0] for sh in shapes])])
+
+    # CPU baseline: the oracle (1 core per process) on one instance per
+    # n-decile, set-up plus a few ADMM iterations, extrapolated with the
+    # iteration count the GPU solve needed for that instance and weighted by
+    # the instances of its decile
+    cpu = None
+    if not args.no_cpu:
+        sample_ids = sorted(kept)
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_iter_sample, [(kept[i], args.cpu_iters) for i in sample_ids], chunksize=1)
+        cpu_secs = time.perf_counter() - t0
+        total = 0.0
+        per = {}
+        for i, (ts, ti) in zip(sample_ids, res):
+            d = samples[i]
+            members = np.nonzero(decile == d)[0]
+            t_inst = ts + ti * float(np.mean(iters[members]))
+            total += t_inst * len(members)
+            per[int(d)] = {"n": int(ns[i]), "setup_s": ts, "s_per_admm_iteration": ti,
+                           "admm_iterations_mean_of_decile": float(np.mean(iters[members]))}
+        cpu = {"value": count / total, "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": f"oracle (C restatement, 1 core per process): one instance per n-decile, set-up + "
+                         f"{args.cpu_iters} ADMM iterations, extrapolated with the decile's mean GPU "
+                         f"iteration count and weighted by its instances ({cpu_secs:.0f} s of sampling)",
+               "deciles": per}
+    pool.close()
+    pool.join()
+
+    # FP64 checks of the FP32 results on the sampled instances: the
+    # single-instance FP64 GPU engine at EPS 1e-7 for every decile, and the
+    # CPU oracle at EPS 1e-8 (CG 200, 1e-12) for the smallest sample
+    checks = []
+    for i in sorted(kept):
+        p = kept[i]
+        got = float(p.c @ x[starts_x[i]:starts_x[i + 1]])
+        with Workspace(p.with_params(EPS_ABS=1e-7, MAX_ITERS=30000, CG_MAX_ITS=40, CG_TOL=1e-10),
+                       "fp64", device=local) as w1:
+            r = w1.solve().fetch()
+        ref = float(p.c @ r["x"])
+        checks.append({"n": int(ns[i]), "class": int(cls[i]), "batch_iters": int(iters[i]),
+                       "fp64_status": r["status"],
+                       "relative_objective_error": abs(got - ref) / max(1.0, abs(ref))})
+    small = min(kept, key=lambda i: ns[i])
+    if not args.no_cpu:
+        from oracle import oracle as O
+        hi = O.port_solve(kept[small].with_params(**TIGHT_ORACLE))
+        ref = float(kept[small].c @ hi["x"])
+        got = float(kept[small].c @ x[starts_x[small]:starts_x[small + 1]])
+        oracle_small = {"n": int(ns[small]), "relative_objective_error": abs(got - ref) / max(1.0, abs(ref))}
+    else:
+        oracle_small = None
+
+    h2d = sum(sh[2] * 16 + (sh[0] + 1) * 8 + (sh[1] + sh[0]) * 8 + 8 for sh in shapes)
+    d2h = sum((sh[0] + 2 * sh[1]) * 8 for sh in shapes)
+    e2e_s = batch.append_seconds + batch.commit_seconds + solve_ms / 1e3 + t_fetch
+    total_nnz = int(sum(sh[2] for sh in shapes))
+    line = {
+        "metric": MIX_METRIC, "value": value, "unit": "solves/s", "n_gpus": ws_n, "steps": 1, "warmup": 0,
+        "ms_per_step": solve_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 reductions)" if sv == 4 else "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "instances_per_step": count, "nnz_per_step": total_nnz,
+                   "n_range": [wl["n_lo"], wl["n_hi"]], "precision": prec, "params": wl["params"],
+                   "waves_of_instances": W, "cta_sizes_by_class": blocks,
+                   "instances_by_class": [int(sum(1 for c in cls if c == k)) for k in range(5)],
+                   "l2": "inputs larger than L2: %.0f GB of A and A' resident in HBM" %
+                         (total_nnz * 2 * (sv + 2) / 1e9),
+                   "parallelism": "one GPU"},
+        "solved": int(sum(d["solved"] for d in inf)), "admm_iterations_mean": float(iters.mean()),
+        "admm_iterations_max": int(iters.max()),
+        "setup": {"append_seconds": batch.append_seconds, "commit_seconds": batch.commit_seconds,
+                  "generation_wait_seconds": t_gen[0], "wall_seconds": t_setup_wall},
+        "fp64_checks": checks, "oracle_check_smallest": oracle_small,
+        "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": {"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "seconds_per_step": e2e_s,
+                "path": "pdosgpu_batch_append of every wave from host arrays (generation excluded), commit, "
+                        "solve, pdosgpu_batch_fetch"},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    batch.close()
+    return 0
+
+
 def run_batch(args, wl):
     import torch
     ws_n, rank, local = dist_env()
@@ -756,6 +946,8 @@ def main():
         wl = BATCH_WORKLOADS[args.workload]
         if args.impl == "reference":
             return run_batch_reference(args, wl)
+        if wl["kind"] == "mix_waves":
+            return run_batch_waves(args, wl)
         if args.profile_iters:
             return profile_batch(args, wl)
         return run_batch(args, wl)

@@ -139,6 +139,22 @@ typedef struct pdosgpu_batch pdosgpu_batch;
 int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count,
                         const pdosgpu_options *opt, int iters_per_launch,
                         pdosgpu_batch **out);
+/* The same set-up in steps, for batches too large to hold on the host at
+ * once: create an empty batch, append problems in any number of calls (each
+ * call's host arrays may be freed once it returns), then commit before the
+ * first solve.  Each append sets its problems up on the device in one or
+ * more waves (at most about 2^30 nonzeros, and a share of the free device
+ * memory, per wave), keeping only the finished layouts and vectors, so the
+ * whole batch may exceed 2^31 nonzeros.  pdosgpu_batch_setup is create +
+ * append + commit; the results do not depend on how the problems were
+ * split into appends.  The per-instance work is the set-up of
+ * pdosgpu_setup (commonWorkInit, common.h:35-218; cs_transpose,
+ * cs.c:146-168). */
+int pdosgpu_batch_create(const pdosgpu_options *opt, int iters_per_launch,
+                         pdosgpu_batch **out);
+int pdosgpu_batch_append(pdosgpu_batch *b, const pdosgpu_problem *probs,
+                         int64_t count);
+int pdosgpu_batch_commit(pdosgpu_batch *b);
 /* Launch until every instance has passed its stop test or run MAX_ITERS. */
 int pdosgpu_batch_solve(pdosgpu_batch *b);
 /* At most `launches` more launches (stops early when all are done). */

@@ -15,6 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(HERE, "lib")
 
 PDOSGPU_OK = 0
+PDOSGPU_EINVAL = -1
+PDOSGPU_ENOMEM = -2
+PDOSGPU_ECUDA = -3
+PDOSGPU_ENOTSUP = -4
 PDOSGPU_FP64 = 0
 PDOSGPU_FP32 = 1
 PDOSGPU_SCALE_2NORM = 0
@@ -79,6 +83,9 @@ SIGNATURES = {
                                               POINTER(c_int64), c_void_p]),
     "pdosgpu_batch_setup": (c_int, [POINTER(Problem), c_int64, POINTER(Options), c_int,
                                     POINTER(c_void_p)]),
+    "pdosgpu_batch_create": (c_int, [POINTER(Options), c_int, POINTER(c_void_p)]),
+    "pdosgpu_batch_append": (c_int, [c_void_p, POINTER(Problem), c_int64]),
+    "pdosgpu_batch_commit": (c_int, [c_void_p]),
     "pdosgpu_batch_solve": (c_int, [c_void_p]),
     "pdosgpu_batch_launch": (c_int, [c_void_p, c_int64]),
     "pdosgpu_batch_reset": (c_int, [c_void_p]),

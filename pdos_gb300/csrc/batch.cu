@@ -53,24 +53,11 @@ constexpr int kSmemLimit = 225 * 1024;  // dynamic shared memory per CTA (opt-in
 constexpr int kBlocks[] = {128, 256, 512, 1024};
 constexpr int kNumBlocks = 4;
 
-struct Inst {
-  int64_t row0, col0;  // offsets into the stacked row / column vectors
-  int32_t m, n, f, l;
-  int64_t cone0;
-  int32_t ncones, cls;
-  Side A, At;
-  double lambda, pscale, dscale, alpha, eps, tol_sq;
-  int64_t max_iters, cg_max;
-};
-
-struct State {
-  double pres_sq, by, p_res, d_res, p_obj, d_obj, eta;
-  long long admm_iter, cg_total;
-  int solved, done, prepped, pad;
-};
-
-template <typename T>
-struct Hyb {
+// Layout arrays of one side (rows of A, or rows of A') of one set-up wave,
+// in device memory.  Every instance carries the arrays of its wave, so the
+// waves of a batch are independent allocations: a batch may hold more than
+// 2^31 nonzeros in all while each wave's set-up keeps 32-bit indices.
+struct HybPtr {
   const int64_t *slice_beg;    // first element of each slice
   const int32_t *slice_w;      // its width (elements per lane)
   const uint32_t *slice_skip;  // lanes whose row is a long row or past the end
@@ -79,7 +66,24 @@ struct Hyb {
   const int32_t *piece_len;
   const int32_t *split_row, *split_p0, *split_np;  // pieces of each split row
   const uint16_t *idx;         // gather index, local to the instance (< 65,536)
-  const T *val;
+  const void *val;             // values (float or double)
+};
+
+struct Inst {
+  int64_t row0, col0;  // offsets into the stacked row / column vectors
+  int32_t m, n, f, l;
+  int64_t cone0;
+  int32_t ncones, cls;
+  Side A, At;
+  double lambda, pscale, dscale, alpha, eps, tol_sq;
+  int64_t max_iters, cg_max;
+  HybPtr hA, hT;  // layout arrays of the instance's wave
+};
+
+struct State {
+  double pres_sq, by, p_res, d_res, p_obj, d_obj, eta;
+  long long admm_iter, cg_total;
+  int solved, done, prepped, pad;
 };
 
 template <typename T>
@@ -92,7 +96,6 @@ struct Dev {
   int32_t *ndone;              // instances finished so far
   T *x, *s, *y, *st, *u, *ax, *q;
   const T *b, *c, *D, *E;
-  Hyb<T> A, At;
   const int32_t *cone_off, *cone_len;  // local first row and size of each cone
   T *gscratch;  // global staging regions of the global class, one per CTA
 };
@@ -218,9 +221,10 @@ __device__ __forceinline__ void fma4(const Idx4 &j, const Val4<T> &v, const T *s
 // lane ([c/4][lane][c%4]), narrower ones one column at a time ([c][lane]).
 // Split rows leave piece partials in pbuf and are finished after a barrier.
 template <typename T, int BLOCK, int NV, class Epi>
-__device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, const T *src0,
+__device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, const T *src0,
                                             const T *src1, T *pbuf, Epi &&epi) {
   constexpr int W = BLOCK / 32;
+  const T *const hval = static_cast<const T *>(H.val);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int k = warp; k < sd.npieces; k += W) {
     const int64_t pk = sd.piece0 + k;
@@ -229,7 +233,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     const int len = H.piece_len[pk];  // a multiple of 4
     T a0 = T(0), a1 = T(0);
     const uint16_t *ip = H.idx + beg;
-    const T *vp = H.val + beg;
+    const T *vp = hval + beg;
 #pragma unroll kUnroll
     for (int e = 4 * lane; e < len; e += 128) {
       const Idx4 j = ld_stream4(ip + e);
@@ -254,7 +258,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
     T a0 = T(0), a1 = T(0);
     if (width < 0) {  // four columns per lane and load
       const uint16_t *ip = H.idx + off + 4 * lane;
-      const T *vp = H.val + off + 4 * lane;
+      const T *vp = hval + off + 4 * lane;
 #pragma unroll kUnroll
       for (int c4 = 0; c4 < -width; c4 += 4) {
         const Idx4 j = ld_stream4(ip + 32 * c4);
@@ -263,7 +267,7 @@ __device__ __forceinline__ void hyb_product(const Hyb<T> &H, const Side &sd, con
       }
     } else {
       const uint16_t *ip = H.idx + off + lane;
-      const T *vp = H.val + off + lane;
+      const T *vp = hval + off + lane;
       for (int c = 0; c < width; ++c) {
         const int j = ip[c * 32];
         const T v = vp[c * 32];
@@ -337,7 +341,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     double red[2] = {0.0, 0.0};
-    hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int r, T a, T) {
+    hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int r, T a, T) {
       ax[r] = a;
       const T sv = s[r], bv = b[r], yv = y[r];
       const T pr = ((sv - bv) + a) / D[r];
@@ -360,7 +364,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     }
     __syncthreads();
     double top[3] = {0.0, 0.0, 0.0};
-    hyb_product<T, BLOCK, 2>(B.At, I.At, g1, g2, pbuf, [&](int j, T sy, T su) {
+    hyb_product<T, BLOCK, 2>(I.hT, I.At, g1, g2, pbuf, [&](int j, T sy, T su) {
       const T cj = c[j];
       const T dr = (cj + sy) / E[j];
       top[0] += (double)dr * (double)dr;
@@ -391,10 +395,10 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       __syncthreads();
     }
     while (active) {
-      hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int r, T a, T) { g2[r] = a; });
+      hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int r, T a, T) { g2[r] = a; });
       __syncthreads();
       double pt[1] = {0.0};
-      hyb_product<T, BLOCK, 1>(B.At, I.At, g2, g2, pbuf, [&](int j, T a, T) {
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, g2, g2, pbuf, [&](int j, T a, T) {
         const T pj = g1[j];
         const T tj = pj + a;
         tt[j] = tj;
@@ -433,7 +437,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     double fin[2] = {0.0, 0.0};
-    hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int r, T a, T) {
+    hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int r, T a, T) {
       T stv = b[r] + (-a);
       stv = alpha * stv + oma * s[r];
       T v = stv - lam * y[r];
@@ -559,15 +563,16 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev
     for (int j = threadIdx.x; j < I.n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     for (int r = 0; r < reps; ++r) {
-      hyb_product<T, BLOCK, 1>(B.A, I.A, g1, g1, pbuf, [&](int row, T a, T) { g2[row] = a; });
+      hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int row, T a, T) { g2[row] = a; });
       __syncthreads();
-      hyb_product<T, BLOCK, 1>(B.At, I.At, g2, g2, pbuf, [&](int j, T a, T) { tt[j] = g1[j] + a; });
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, g2, g2, pbuf, [&](int j, T a, T) { tt[j] = g1[j] + a; });
       __syncthreads();
     }
   }
 }
 
 static_assert(sizeof(Inst) % 4 == 0 && sizeof(Inst) / 4 <= 128, "Inst is copied by one 128-thread pass");
+static_assert(alignof(Inst) == 8, "Inst is copied as 32-bit words into an 8-byte aligned slot");
 
 // y = D y-unscale etc. (pdos.c:261-294) over the stacked vectors.
 template <typename T>
@@ -613,52 +618,51 @@ __global__ void gather_values_kernel(const int32_t *src, int64_t count, const T 
 }
 
 // ------------------------------------------------------------ host side
+// Uploads one side's layout of one wave; values are gathered on the device
+// from the wave's (scaled) value array through the layout's source map.
 template <typename T>
-struct HybDevOwned {
-  Hyb<T> h{};
-  int upload(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStream_t st) {
-    auto up = [&](auto **dst, const auto &v) -> int {
-      using E = typename std::decay_t<decltype(v)>::value_type;
-      E *p = nullptr;
-      PDOS_TRY(arena.alloc(&p, v.size() + 1));
-      if (!v.empty())
-        PDOS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice, st));
-      *dst = p;
-      return PDOSGPU_OK;
-    };
-    int64_t *slice_beg, *piece_beg;
-    uint32_t *slice_skip;
-    int32_t *slice_w, *piece_row, *piece_len, *split_row, *split_p0, *split_np;
-    uint16_t *idx;
-    PDOS_TRY(up(&slice_beg, hb.slice_beg));
-    PDOS_TRY(up(&slice_w, hb.slice_w));
-    PDOS_TRY(up(&slice_skip, hb.slice_skip));
-    PDOS_TRY(up(&piece_row, hb.piece_row));
-    PDOS_TRY(up(&piece_beg, hb.piece_beg));
-    PDOS_TRY(up(&piece_len, hb.piece_len));
-    PDOS_TRY(up(&split_row, hb.split_row));
-    PDOS_TRY(up(&split_p0, hb.split_p0));
-    PDOS_TRY(up(&split_np, hb.split_np));
-    PDOS_TRY(up(&idx, hb.idx));
-    T *val = nullptr;
-    PDOS_TRY(arena.alloc(&val, hb.src.size() + 1));
-    if (!hb.src.empty()) {
-      DeviceArena tmp;
-      int32_t *src = nullptr;
-      PDOS_TRY(tmp.alloc(&src, hb.src.size()));
-      PDOS_CUDA_TRY(cudaMemcpyAsync(src, hb.src.data(), sizeof(int32_t) * hb.src.size(),
-                                    cudaMemcpyHostToDevice, st));
-      const int64_t cnt = (int64_t)hb.src.size();
-      const int g = (int)std::min<int64_t>((cnt + 255) / 256, (int64_t)num_sms() * 16);
-      gather_values_kernel<T><<<g, 256, 0, st>>>(src, cnt, values, val);
-      PDOS_CUDA_TRY(cudaGetLastError());
-      PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before src is freed
-    }
-    h = Hyb<T>{slice_beg, slice_w, slice_skip, piece_row, piece_beg, piece_len, split_row, split_p0,
-               split_np, idx, val};
+int upload_hyb(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStream_t st, HybPtr &h) {
+  auto up = [&](auto **dst, const auto &v) -> int {
+    using E = typename std::decay_t<decltype(v)>::value_type;
+    E *p = nullptr;
+    PDOS_TRY(arena.alloc(&p, v.size() + 1));
+    if (!v.empty())
+      PDOS_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice, st));
+    *dst = p;
     return PDOSGPU_OK;
+  };
+  int64_t *slice_beg, *piece_beg;
+  uint32_t *slice_skip;
+  int32_t *slice_w, *piece_row, *piece_len, *split_row, *split_p0, *split_np;
+  uint16_t *idx;
+  PDOS_TRY(up(&slice_beg, hb.slice_beg));
+  PDOS_TRY(up(&slice_w, hb.slice_w));
+  PDOS_TRY(up(&slice_skip, hb.slice_skip));
+  PDOS_TRY(up(&piece_row, hb.piece_row));
+  PDOS_TRY(up(&piece_beg, hb.piece_beg));
+  PDOS_TRY(up(&piece_len, hb.piece_len));
+  PDOS_TRY(up(&split_row, hb.split_row));
+  PDOS_TRY(up(&split_p0, hb.split_p0));
+  PDOS_TRY(up(&split_np, hb.split_np));
+  PDOS_TRY(up(&idx, hb.idx));
+  T *val = nullptr;
+  PDOS_TRY(arena.alloc(&val, hb.src.size() + 1));
+  if (!hb.src.empty()) {
+    DeviceArena tmp;
+    int32_t *src = nullptr;
+    PDOS_TRY(tmp.alloc(&src, hb.src.size()));
+    PDOS_CUDA_TRY(cudaMemcpyAsync(src, hb.src.data(), sizeof(int32_t) * hb.src.size(),
+                                  cudaMemcpyHostToDevice, st));
+    const int64_t cnt = (int64_t)hb.src.size();
+    const int g = (int)std::min<int64_t>((cnt + 255) / 256, (int64_t)num_sms() * 16);
+    gather_values_kernel<T><<<g, 256, 0, st>>>(src, cnt, values, val);
+    PDOS_CUDA_TRY(cudaGetLastError());
+    PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before src (and the host arrays) are freed
   }
-};
+  h = HybPtr{slice_beg, slice_w, slice_skip, piece_row, piece_beg, piece_len, split_row, split_p0,
+             split_np, idx, val};
+  return PDOSGPU_OK;
+}
 
 inline double now_ms() {
   using namespace std::chrono;
@@ -694,6 +698,8 @@ KernelOf<T> products_kernel_for(int block, bool global) {
 class BatchBase {
  public:
   virtual ~BatchBase() {}
+  virtual int append(const pdosgpu_problem *probs, int64_t count) = 0;
+  virtual int commit() = 0;
   virtual int solve(int64_t max_launches) = 0;
   virtual int reset() = 0;
   virtual int warm_start(const double *x0, const double *y0, const double *s0) = 0;
@@ -705,11 +711,30 @@ class BatchBase {
   virtual int set_blocks(const int *blocks) = 0;
   virtual void *stream() = 0;
   virtual int64_t done_count() = 0;
-  int64_t count = 0, total_n = 0, total_m = 0, total_nnz = 0;
+  bool committed = false;
+  int64_t count = 0, total_n = 0, total_m = 0, total_nnz = 0, waves = 0;
   double setup_ms = 0, solve_ms = 0;
   int64_t launches = 0;
-  std::vector<int64_t> row0, col0;
+  std::vector<int64_t> row0{0}, col0{0};
 };
+
+// Device vectors of one wave, kept until commit() stacks every wave's.
+template <typename T>
+struct WaveVectors {
+  DeviceArena arena;
+  int64_t n = 0, m = 0, col0 = 0, row0 = 0;
+  T *b = nullptr, *c = nullptr, *D = nullptr, *E = nullptr;
+  T *x_init = nullptr, *y_init = nullptr, *s_init = nullptr;
+  double *D64 = nullptr, *E64 = nullptr, *Epre64 = nullptr;
+};
+
+// Nonzeros a wave may hold: its stacked set-up keeps 32-bit indices, and
+// its transient device memory (the problem in double and 64-bit indices,
+// the CSC -> CSR transpose, the scaled values, both layouts) is bounded by
+// a share of the free device memory.
+constexpr int64_t kWaveMaxNnz = ((int64_t)1 << 30);
+constexpr int64_t kWaveMaxVec = (int64_t)INT32_MAX - 4096;
+constexpr int64_t kSetupBytesPerNnz = 128;
 
 template <typename T>
 class BatchEngine : public BatchBase {
@@ -728,7 +753,9 @@ class BatchEngine : public BatchBase {
     if (host_done_) cudaFreeHost(host_done_);
   }
 
-  int setup(const pdosgpu_problem *probs, int64_t count_in, const pdosgpu_options &opt, int iter_cap);
+  int create(const pdosgpu_options &opt, int iter_cap);
+  int append(const pdosgpu_problem *probs, int64_t count_in) override;
+  int commit() override;
   int solve(int64_t max_launches) override;
   int reset() override;
   int warm_start(const double *x0, const double *y0, const double *s0) override;
@@ -741,13 +768,18 @@ class BatchEngine : public BatchBase {
   int64_t done_count() override;
 
  private:
+  int append_wave(const pdosgpu_problem *probs, int64_t cnt);
   int build_graph(int iter_cap, cudaGraphExec_t *exec);
   int configure(int cls, int block);
   int launch_class(int cls, int block, int iter_cap, cudaStream_t st);
   int grid_[kClasses]{};
   int64_t active_launch_nodes_ = 0;
 
-  DeviceArena arena_;
+  pdosgpu_options opt_{};
+  int normalize_ = -1;              // NORMALIZE shared by every instance (-1: none yet)
+  DeviceArena arena_;               // stacked vectors, instance tables, scratch
+  std::vector<std::unique_ptr<DeviceArena>> layout_arenas_;  // one per wave: its layouts
+  std::vector<std::unique_ptr<WaveVectors<T>>> wave_vecs_;   // until commit()
   cudaStream_t stream_ = nullptr;
   std::vector<cudaStream_t> side_;
   std::vector<cudaEvent_t> ev_;
@@ -755,7 +787,6 @@ class BatchEngine : public BatchBase {
   int iter_cap_ = 64;
   int gregions_ = 0;  // staging regions allocated for the global class
   Dev<T> dev_{};
-  HybDevOwned<T> hA_, hT_;
   Inst *inst_d_ = nullptr;
   State *state_d_ = nullptr;
   int32_t *queue_ = nullptr, *ndone_ = nullptr;
@@ -763,55 +794,93 @@ class BatchEngine : public BatchBase {
   std::vector<Inst> inst_h_;
   std::vector<int64_t> nnz_h_;
   std::vector<int32_t> class_begin_h_;
+  std::vector<int32_t> cone_off_h_, cone_len_h_;
   Smem smem_[kClasses]{};
   int block_[kClasses]{};
   T *x_init_ = nullptr, *y_init_ = nullptr, *s_init_ = nullptr;
   double *D64_ = nullptr, *E64_ = nullptr, *Epre64_ = nullptr, *out_ = nullptr;
-  double *warm_[3] = {nullptr, nullptr, nullptr};
 };
 
 template <typename T>
-int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosgpu_options &opt,
-                          int iter_cap) {
-  const double t0 = now_ms();
-  if (cnt <= 0 || cnt > (int64_t)INT32_MAX / 2) return fail(PDOSGPU_EINVAL, "batch count out of range");
+int BatchEngine<T>::create(const pdosgpu_options &opt, int iter_cap) {
   if (iter_cap <= 0) return fail(PDOSGPU_EINVAL, "iterations per launch must be positive");
   iter_cap_ = iter_cap;
-  count = cnt;
-  int64_t N = 0, M = 0, NNZ = 0, ncones = 0;
-  bool any_x = false, any_y = false, any_s = false;
+  opt_ = opt;
+  PDOS_CUDA_TRY(cudaSetDevice(opt.device));
+  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  return PDOSGPU_OK;
+}
+
+// Appends problems in as many waves as the limits on one wave require.
+template <typename T>
+int BatchEngine<T>::append(const pdosgpu_problem *probs, int64_t cnt) {
+  const double t0 = now_ms();
+  if (committed) return fail(PDOSGPU_EINVAL, "the batch is already committed");
+  if (cnt <= 0 || count + cnt > (int64_t)INT32_MAX / 2) return fail(PDOSGPU_EINVAL, "batch count out of range");
   for (int64_t i = 0; i < cnt; ++i) {
     const pdosgpu_problem &p = probs[i];
     const int rc = validate_problem(p);
-    if (rc != PDOSGPU_OK) return fail(rc, "instance " + std::to_string(i) + ": " + pdos_gpu_last_error());
+    if (rc != PDOSGPU_OK)
+      return fail(rc, "instance " + std::to_string(count + i) + ": " + pdos_gpu_last_error());
     if (p.m > 65535 || p.n > 65535)
-      return fail(PDOSGPU_ENOTSUP, "instance " + std::to_string(i) +
+      return fail(PDOSGPU_ENOTSUP, "instance " + std::to_string(count + i) +
                                        " is too large for the batch's 16-bit instance-local indices "
                                        "(m and n must stay below 65,536); solve it with pdosgpu_setup");
-    if ((p.normalize != 0) != (probs[0].normalize != 0))
+    if (normalize_ < 0) normalize_ = p.normalize ? 1 : 0;
+    if ((p.normalize != 0) != (normalize_ != 0))
       return fail(PDOSGPU_EINVAL, "all instances of a batch must share NORMALIZE");
-    row0.push_back(M);
-    col0.push_back(N);
+  }
+  if (normalize_ && opt_.scaling == PDOSGPU_SCALE_RUIZ)
+    return fail(PDOSGPU_ENOTSUP, "Ruiz equilibration is not available for batches");
+  PDOS_CUDA_TRY(cudaSetDevice(opt_.device));
+  size_t free_b = 0, total_b = 0;
+  PDOS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+  const int64_t max_nnz =
+      std::max<int64_t>(1, std::min<int64_t>(kWaveMaxNnz, (int64_t)(free_b / 2 / kSetupBytesPerNnz)));
+  int64_t first = 0;
+  while (first < cnt) {
+    int64_t last = first, nz = 0, n = 0, m = 0;
+    do {  // at least one instance per wave
+      nz += probs[last].Ap[probs[last].n];
+      n += probs[last].n;
+      m += probs[last].m;
+      ++last;
+    } while (last < cnt && nz + probs[last].Ap[probs[last].n] <= max_nnz &&
+             n + probs[last].n <= kWaveMaxVec && m + probs[last].m <= kWaveMaxVec);
+    PDOS_TRY(append_wave(probs + first, last - first));
+    first = last;
+  }
+  setup_ms += now_ms() - t0;
+  return PDOSGPU_OK;
+}
+
+// One wave: stack its instances block-diagonally on the host, set them up on
+// the device (transpose, equilibration, warm start, lambda; every row,
+// column and cone is scaled exactly as when the instance is alone), build
+// both sides' layouts, upload them into the wave's own allocation, and keep
+// the wave's vectors until commit().
+template <typename T>
+int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
+  int64_t N = 0, M = 0, NNZ = 0;
+  bool any_x = false, any_y = false, any_s = false;
+  std::vector<int64_t> wrow0, wcol0;  // offsets inside the wave
+  for (int64_t i = 0; i < cnt; ++i) {
+    const pdosgpu_problem &p = probs[i];
+    wrow0.push_back(M);
+    wcol0.push_back(N);
     N += p.n;
     M += p.m;
     NNZ += p.Ap[p.n];
-    ncones += p.qsize;
     any_x |= p.x0 != nullptr;
     any_y |= p.y0 != nullptr;
     any_s |= p.s0 != nullptr;
   }
-  row0.push_back(M);
-  col0.push_back(N);
-  const int64_t lim = (int64_t)INT32_MAX - 4096;
-  if (N > lim || M > lim || NNZ > lim)
-    return fail(PDOSGPU_EINVAL, "stacked m, n and nnz must each be below 2^31 - 4096");
-  if (probs[0].normalize && opt.scaling == PDOSGPU_SCALE_RUIZ)
-    return fail(PDOSGPU_ENOTSUP, "Ruiz equilibration is not available for batches");
-  total_n = N;
-  total_m = M;
-  total_nnz = NNZ;
+  wrow0.push_back(M);
+  wcol0.push_back(N);
+  if (N > kWaveMaxVec || M > kWaveMaxVec || NNZ > kWaveMaxVec)
+    return fail(PDOSGPU_EINVAL, "an instance is too large for one set-up wave (2^31 - 4096 nonzeros)");
 
-  // ---- stacked problem (block diagonal), host
+  // ---- stacked problem of the wave (block diagonal), host
   Raw<double> Ax, b, c;
   Raw<int64_t> Ai, Ap;
   Ax.resize(NNZ);
@@ -829,7 +898,7 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     for (int64_t i = 0; i < cnt; ++i) {
       const pdosgpu_problem &p = probs[i];
       e0[i + 1] = e0[i] + p.Ap[p.n];
-      int64_t off = row0[i] + p.f + p.l;
+      int64_t off = wrow0[i] + p.f + p.l;
       for (int64_t k = 0; k < p.qsize; ++k) {
         d.soc_off.push_back(off);
         d.soc_len.push_back(p.q[k]);
@@ -839,14 +908,14 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     parallel_for(cnt, [&](int64_t i) {
       const pdosgpu_problem &p = probs[i];
       const int64_t nz = p.Ap[p.n], e = e0[i];
-      for (int64_t j = 0; j < p.n; ++j) Ap[col0[i] + j] = e + p.Ap[j];
+      for (int64_t j = 0; j < p.n; ++j) Ap[wcol0[i] + j] = e + p.Ap[j];
       if (nz > 0) std::memcpy(&Ax[e], p.Ax, sizeof(double) * nz);
-      for (int64_t k = 0; k < nz; ++k) Ai[e + k] = row0[i] + p.Ai[k];
-      std::memcpy(&b[row0[i]], p.b, sizeof(double) * p.m);
-      std::memcpy(&c[col0[i]], p.c, sizeof(double) * p.n);
-      if (p.x0) std::memcpy(&x0[col0[i]], p.x0, sizeof(double) * p.n);
-      if (p.y0) std::memcpy(&y0[row0[i]], p.y0, sizeof(double) * p.m);
-      if (p.s0) std::memcpy(&s0[row0[i]], p.s0, sizeof(double) * p.m);
+      for (int64_t k = 0; k < nz; ++k) Ai[e + k] = wrow0[i] + p.Ai[k];
+      std::memcpy(&b[wrow0[i]], p.b, sizeof(double) * p.m);
+      std::memcpy(&c[wcol0[i]], p.c, sizeof(double) * p.n);
+      if (p.x0) std::memcpy(&x0[wcol0[i]], p.x0, sizeof(double) * p.n);
+      if (p.y0) std::memcpy(&y0[wrow0[i]], p.y0, sizeof(double) * p.m);
+      if (p.s0) std::memcpy(&s0[wrow0[i]], p.s0, sizeof(double) * p.m);
     });
     Ap[N] = e0[cnt];
   }
@@ -861,21 +930,39 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   d.x0 = any_x ? x0.data() : nullptr;
   d.y0 = any_y ? y0.data() : nullptr;
   d.s0 = any_s ? s0.data() : nullptr;
-  d.inst_row0 = row0;
-  d.inst_col0 = col0;
-  d.normalize = probs[0].normalize ? 1 : 0;
+  d.inst_row0 = wrow0;
+  d.inst_col0 = wcol0;
+  d.normalize = normalize_;
 
-  PDOS_CUDA_TRY(cudaSetDevice(opt.device));
-  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   cudaStream_t st = stream_;
+  DeviceArena setup_arena;  // the wave's set-up arrays, released at the end of the wave
   DeviceProblem<T> P;
-  PDOS_TRY(setup_problem<T>(d, arena_, st, P));
-  D64_ = P.D64;
-  E64_ = P.E64;
-  Epre64_ = P.Epre64;
-  x_init_ = P.x_init;
-  y_init_ = P.y_init;
-  s_init_ = P.s_init;
+  PDOS_TRY(setup_problem<T>(d, setup_arena, st, P));
+
+  // ---- the wave's vectors, kept until commit()
+  auto wv = std::make_unique<WaveVectors<T>>();
+  wv->n = N;
+  wv->m = M;
+  wv->col0 = total_n;
+  wv->row0 = total_m;
+  auto keep = [&](auto **dst, const auto *from, int64_t len) -> int {
+    using E = std::remove_const_t<std::remove_pointer_t<std::decay_t<decltype(from)>>>;
+    E *p = nullptr;
+    PDOS_TRY(wv->arena.alloc(&p, (size_t)len));
+    if (len > 0) PDOS_CUDA_TRY(cudaMemcpyAsync(p, from, sizeof(E) * len, cudaMemcpyDeviceToDevice, st));
+    *dst = p;
+    return PDOSGPU_OK;
+  };
+  PDOS_TRY(keep(&wv->b, P.b, M));
+  PDOS_TRY(keep(&wv->c, P.c, N));
+  PDOS_TRY(keep(&wv->D, P.D, M));
+  PDOS_TRY(keep(&wv->E, P.E, N));
+  PDOS_TRY(keep(&wv->x_init, P.x_init, N));
+  PDOS_TRY(keep(&wv->y_init, P.y_init, M));
+  PDOS_TRY(keep(&wv->s_init, P.s_init, M));
+  PDOS_TRY(keep(&wv->D64, P.D64, M));
+  PDOS_TRY(keep(&wv->E64, P.E64, N));
+  PDOS_TRY(keep(&wv->Epre64, P.Epre64, N));
 
   // ---- hybrid layouts of both sides, instance by instance
   Raw<int32_t> Rj;
@@ -883,28 +970,24 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   if (NNZ > 0)
     PDOS_CUDA_TRY(cudaMemcpyAsync(Rj.data(), P.Rj, sizeof(int32_t) * NNZ, cudaMemcpyDeviceToHost, st));
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-  HybBuild bA, bT;
-  inst_h_.assign(cnt, Inst{});
-  std::vector<int32_t> cone_off_h, cone_len_h;
-  int64_t cone_pos = 0;
+  const int64_t first = count;
   for (int64_t i = 0; i < cnt; ++i) {
     const pdosgpu_problem &p = probs[i];
-    Inst &I = inst_h_[i];
-    I.row0 = row0[i];
-    I.col0 = col0[i];
+    Inst I{};
+    I.row0 = total_m + wrow0[i];
+    I.col0 = total_n + wcol0[i];
     I.m = (int32_t)p.m;
     I.n = (int32_t)p.n;
     I.f = (int32_t)p.f;
     I.l = (int32_t)p.l;
-    I.cone0 = cone_pos;
+    I.cone0 = (int64_t)cone_off_h_.size();
     I.ncones = (int32_t)p.qsize;
     int64_t off = p.f + p.l;
     for (int64_t k = 0; k < p.qsize; ++k) {
-      cone_off_h.push_back((int32_t)off);
-      cone_len_h.push_back((int32_t)p.q[k]);
+      cone_off_h_.push_back((int32_t)off);
+      cone_len_h_.push_back((int32_t)p.q[k]);
       off += p.q[k];
     }
-    cone_pos += p.qsize;
     I.lambda = P.lambda[i];
     I.pscale = P.pscale[i];
     I.dscale = P.dscale[i];
@@ -918,8 +1001,13 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     int cls = 0;
     while (cls < 3 && nz > kClassNnz[cls]) ++cls;
     I.cls = cls;
+    inst_h_.push_back(I);
+    row0.push_back(I.row0 + p.m);
+    col0.push_back(I.col0 + p.n);
   }
+  auto arena = std::make_unique<DeviceArena>();
   {
+    HybBuild bA, bT;
     std::vector<Side> sides;
     const int32_t *rp = P.rp_host.data(), *ap = P.ap_host.data();
     const int32_t *rj = Rj.data();
@@ -928,42 +1016,105 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
                                        int64_t &r1, int64_t &c0) {
       ptr = rp;
       g = rj;
-      r0 = row0[i];
-      r1 = row0[i + 1];
-      c0 = col0[i];
+      r0 = wrow0[i];
+      r1 = wrow0[i + 1];
+      c0 = wcol0[i];
     }, sides);
-    for (int64_t i = 0; i < cnt; ++i) inst_h_[i].A = sides[i];
+    for (int64_t i = 0; i < cnt; ++i) inst_h_[first + i].A = sides[i];
     build_layout<int64_t>(bT, cnt, [&](int64_t i, const int32_t *&ptr, const int64_t *&g, int64_t &r0,
                                        int64_t &r1, int64_t &c0) {
       ptr = ap;
       g = ai;
-      r0 = col0[i];
-      r1 = col0[i + 1];
-      c0 = row0[i];
+      r0 = wcol0[i];
+      r1 = wcol0[i + 1];
+      c0 = wrow0[i];
     }, sides);
-    for (int64_t i = 0; i < cnt; ++i) inst_h_[i].At = sides[i];
+    for (int64_t i = 0; i < cnt; ++i) inst_h_[first + i].At = sides[i];
+    HybPtr hA{}, hT{};
+    PDOS_TRY(upload_hyb<T>(bA, P.Rx, *arena, st, hA));
+    PDOS_TRY(upload_hyb<T>(bT, P.Ax, *arena, st, hT));
+    for (int64_t i = 0; i < cnt; ++i) {
+      inst_h_[first + i].hA = hA;
+      inst_h_[first + i].hT = hT;
+    }
   }
-  PDOS_TRY(hA_.upload(bA, P.Rx, arena_, st));
-  PDOS_TRY(hT_.upload(bT, P.Ax, arena_, st));
-
-  // ---- classes: staging regions and the processing order (largest
-  // instances first within a class); an instance whose own regions exceed
-  // one CTA's shared memory goes to the global class
+  // an instance whose own staging regions exceed one CTA's shared memory
+  // goes to the global class
   auto r4 = [](int32_t v) { return (v + 3) & ~3; };
   for (int64_t i = 0; i < cnt; ++i) {
-    Inst &I = inst_h_[i];
+    Inst &I = inst_h_[first + i];
     const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0};
     if (own.need(sizeof(T)) > (size_t)kSmemLimit) I.cls = kGlobalClass;
   }
+  PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // the wave's set-up arrays are released next
+  layout_arenas_.push_back(std::move(arena));
+  wave_vecs_.push_back(std::move(wv));
+  count += cnt;
+  total_n += N;
+  total_m += M;
+  total_nnz += NNZ;
+  ++waves;
+  return PDOSGPU_OK;
+}
+
+// Stacks the waves' vectors, sorts the instances into size classes, uploads
+// the instance tables and captures the launch graph.
+template <typename T>
+int BatchEngine<T>::commit() {
+  const double t0 = now_ms();
+  if (committed) return fail(PDOSGPU_EINVAL, "the batch is already committed");
+  if (count == 0) return fail(PDOSGPU_EINVAL, "batch count out of range");
+  cudaStream_t st = stream_;
+  const int64_t N = total_n, M = total_m;
+  Dev<T> &B = dev_;
+  {  // stacked vectors
+    T *b, *c, *D, *E;
+    PDOS_TRY(arena_.alloc(&b, (size_t)M));
+    PDOS_TRY(arena_.alloc(&c, (size_t)N));
+    PDOS_TRY(arena_.alloc(&D, (size_t)M));
+    PDOS_TRY(arena_.alloc(&E, (size_t)N));
+    PDOS_TRY(arena_.alloc(&x_init_, (size_t)N));
+    PDOS_TRY(arena_.alloc(&y_init_, (size_t)M));
+    PDOS_TRY(arena_.alloc(&s_init_, (size_t)M));
+    PDOS_TRY(arena_.alloc(&D64_, (size_t)M));
+    PDOS_TRY(arena_.alloc(&E64_, (size_t)N));
+    PDOS_TRY(arena_.alloc(&Epre64_, (size_t)N));
+    for (auto &w : wave_vecs_) {
+      auto cp = [&](auto *dst, const auto *from, int64_t off, int64_t len) -> int {
+        if (len > 0)
+          PDOS_CUDA_TRY(cudaMemcpyAsync(dst + off, from, sizeof(*from) * len, cudaMemcpyDeviceToDevice, st));
+        return PDOSGPU_OK;
+      };
+      PDOS_TRY(cp(b, w->b, w->row0, w->m));
+      PDOS_TRY(cp(c, w->c, w->col0, w->n));
+      PDOS_TRY(cp(D, w->D, w->row0, w->m));
+      PDOS_TRY(cp(E, w->E, w->col0, w->n));
+      PDOS_TRY(cp(x_init_, w->x_init, w->col0, w->n));
+      PDOS_TRY(cp(y_init_, w->y_init, w->row0, w->m));
+      PDOS_TRY(cp(s_init_, w->s_init, w->row0, w->m));
+      PDOS_TRY(cp(D64_, w->D64, w->row0, w->m));
+      PDOS_TRY(cp(E64_, w->E64, w->col0, w->n));
+      PDOS_TRY(cp(Epre64_, w->Epre64, w->col0, w->n));
+    }
+    PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+    wave_vecs_.clear();
+    B.b = b;
+    B.c = c;
+    B.D = D;
+    B.E = E;
+  }
+
+  // ---- classes: staging regions and the processing order (largest
+  // instances first within a class)
+  const int64_t cnt = count;
+  auto r4 = [](int32_t v) { return (v + 3) & ~3; };
   std::vector<std::vector<int32_t>> members(kClasses);
   for (int64_t i = 0; i < cnt; ++i) members[inst_h_[i].cls].push_back((int32_t)i);
   std::vector<int32_t> order;
   class_begin_h_.assign(kClasses + 1, 0);
   for (int k = 0; k < kClasses; ++k) {
     auto &mv = members[k];
-    std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) {
-      return probs[a].Ap[probs[a].n] > probs[bb].Ap[probs[bb].n];
-    });
+    std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) { return nnz_h_[a] > nnz_h_[bb]; });
     Smem sm{0, 0, 0, 0, k == kGlobalClass ? 1 : 0};
     for (int32_t i : mv) {
       const Inst &I = inst_h_[i];
@@ -987,19 +1138,18 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   PDOS_TRY(arena_.alloc(&class_begin_d, (size_t)kClasses + 1));
   PDOS_TRY(arena_.alloc(&queue_, (size_t)kClasses + 1));
   ndone_ = queue_ + kClasses;
-  PDOS_TRY(arena_.alloc(&cone_off_d, cone_off_h.size() + 1));
-  PDOS_TRY(arena_.alloc(&cone_len_d, cone_len_h.size() + 1));
+  PDOS_TRY(arena_.alloc(&cone_off_d, cone_off_h_.size() + 1));
+  PDOS_TRY(arena_.alloc(&cone_len_d, cone_len_h_.size() + 1));
   PDOS_CUDA_TRY(cudaMemcpyAsync(inst_d_, inst_h_.data(), sizeof(Inst) * cnt, cudaMemcpyHostToDevice, st));
   PDOS_CUDA_TRY(cudaMemcpyAsync(order_d, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, st));
   PDOS_CUDA_TRY(cudaMemcpyAsync(class_begin_d, class_begin_h_.data(), sizeof(int32_t) * (kClasses + 1),
                                 cudaMemcpyHostToDevice, st));
-  if (!cone_off_h.empty()) {
-    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_off_d, cone_off_h.data(), sizeof(int32_t) * cone_off_h.size(),
+  if (!cone_off_h_.empty()) {
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_off_d, cone_off_h_.data(), sizeof(int32_t) * cone_off_h_.size(),
                                   cudaMemcpyHostToDevice, st));
-    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_len_d, cone_len_h.data(), sizeof(int32_t) * cone_len_h.size(),
+    PDOS_CUDA_TRY(cudaMemcpyAsync(cone_len_d, cone_len_h_.data(), sizeof(int32_t) * cone_len_h_.size(),
                                   cudaMemcpyHostToDevice, st));
   }
-  Dev<T> &B = dev_;
   B.inst = inst_d_;
   B.state = state_d_;
   B.order = order_d;
@@ -1013,18 +1163,12 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
   PDOS_TRY(arena_.alloc(&B.st, (size_t)M));
   PDOS_TRY(arena_.alloc(&B.u, (size_t)M));
   PDOS_TRY(arena_.alloc(&B.ax, (size_t)M));
-  B.b = P.b;
-  B.c = P.c;
-  B.D = P.D;
-  B.E = P.E;
-  B.A = hA_.h;
-  B.At = hT_.h;
   B.cone_off = cone_off_d;
   B.cone_len = cone_len_d;
   B.gscratch = nullptr;
   {  // one staging region per resident CTA of the global class (at most 8 per SM)
-    const int members = class_begin_h_[kGlobalClass + 1] - class_begin_h_[kGlobalClass];
-    gregions_ = std::min(members, num_sms() * (1024 / kBlocks[0]));
+    const int members_g = class_begin_h_[kGlobalClass + 1] - class_begin_h_[kGlobalClass];
+    gregions_ = std::min(members_g, num_sms() * (1024 / kBlocks[0]));
     if (gregions_ > 0) PDOS_TRY(arena_.alloc(&B.gscratch, (size_t)gregions_ * smem_[kGlobalClass].stride()));
   }
   PDOS_TRY(arena_.alloc(&out_, (size_t)N + 2 * (size_t)M));
@@ -1044,11 +1188,12 @@ int BatchEngine<T>::setup(const pdosgpu_problem *probs, int64_t cnt, const pdosg
     ev_.push_back(e);  // fork event
   }
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
+  committed = true;
   PDOS_TRY(reset());
   exec_.assign(1, nullptr);
   PDOS_TRY(build_graph(iter_cap_, &exec_[0]));
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-  setup_ms = now_ms() - t0;
+  setup_ms += now_ms() - t0;
   return PDOSGPU_OK;
 }
 
@@ -1372,9 +1517,8 @@ using namespace pdosgpu;
 
 extern "C" {
 
-int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count, const pdosgpu_options *opt,
-                        int iters_per_launch, pdosgpu_batch **out) {
-  if (!probs || !out) return fail(PDOSGPU_EINVAL, "NULL argument");
+int pdosgpu_batch_create(const pdosgpu_options *opt, int iters_per_launch, pdosgpu_batch **out) {
+  if (!out) return fail(PDOSGPU_EINVAL, "NULL argument");
   *out = nullptr;
   int devs = 0;
   cudaError_t e = cudaGetDeviceCount(&devs);
@@ -1389,11 +1533,11 @@ int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count, const pdosg
   if (iters_per_launch <= 0) iters_per_launch = INT32_MAX;  // each instance runs to its end
   if (o.precision == PDOSGPU_FP32) {
     auto b = std::make_unique<batch::BatchEngine<float>>();
-    rc = b->setup(probs, count, o, iters_per_launch);
+    rc = b->create(o, iters_per_launch);
     if (rc == PDOSGPU_OK) w->engine = std::move(b);
   } else if (o.precision == PDOSGPU_FP64) {
     auto b = std::make_unique<batch::BatchEngine<double>>();
-    rc = b->setup(probs, count, o, iters_per_launch);
+    rc = b->create(o, iters_per_launch);
     if (rc == PDOSGPU_OK) w->engine = std::move(b);
   } else {
     rc = fail(PDOSGPU_EINVAL, "unknown precision");
@@ -1406,50 +1550,84 @@ int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count, const pdosg
   return PDOSGPU_OK;
 }
 
-int pdosgpu_batch_solve(pdosgpu_batch *b) {
+int pdosgpu_batch_append(pdosgpu_batch *b, const pdosgpu_problem *probs, int64_t count) {
+  if (!b || !b->engine || !probs) return fail(PDOSGPU_EINVAL, "NULL argument");
+  return b->engine->append(probs, count);
+}
+
+int pdosgpu_batch_commit(pdosgpu_batch *b) {
   if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  return b->engine->commit();
+}
+
+int pdosgpu_batch_setup(const pdosgpu_problem *probs, int64_t count, const pdosgpu_options *opt,
+                        int iters_per_launch, pdosgpu_batch **out) {
+  if (!probs || !out) return fail(PDOSGPU_EINVAL, "NULL argument");
+  *out = nullptr;
+  pdosgpu_batch *w = nullptr;
+  PDOS_TRY(pdosgpu_batch_create(opt, iters_per_launch, &w));
+  int rc = pdosgpu_batch_append(w, probs, count);
+  if (rc == PDOSGPU_OK) rc = pdosgpu_batch_commit(w);
+  if (rc != PDOSGPU_OK) {
+    delete w;
+    return rc;
+  }
+  *out = w;
+  return PDOSGPU_OK;
+}
+
+// A batch in use: created and committed.
+static int ready(pdosgpu_batch *b) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  if (!b->engine->committed) return fail(PDOSGPU_EINVAL, "the batch is not committed (pdosgpu_batch_commit)");
+  return PDOSGPU_OK;
+}
+
+int pdosgpu_batch_solve(pdosgpu_batch *b) {
+  PDOS_TRY(ready(b));
   return b->engine->solve(-1);
 }
 
 int pdosgpu_batch_launch(pdosgpu_batch *b, int64_t launches) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   if (launches < 0) return fail(PDOSGPU_EINVAL, "launches must be nonnegative");
   return b->engine->solve(launches);
 }
 
 int pdosgpu_batch_reset(pdosgpu_batch *b) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   return b->engine->reset();
 }
 
 int pdosgpu_batch_warm_start(pdosgpu_batch *b, const double *x0, const double *y0, const double *s0) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   return b->engine->warm_start(x0, y0, s0);
 }
 
 int pdosgpu_batch_fetch(pdosgpu_batch *b, int64_t first, int64_t count, double *x, double *s,
                         double *y, pdosgpu_info *info) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   return b->engine->fetch(first, count, x, s, y, info);
 }
 
 int64_t pdosgpu_batch_done(pdosgpu_batch *b) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   return b->engine->done_count();
 }
 
 int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   return b->engine->tune(iters, blocks);
 }
 
 int pdosgpu_batch_time_products(pdosgpu_batch *b, int reps, double *ms, double *bytes) {
-  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  PDOS_TRY(ready(b));
   return b->engine->time_products(reps, ms, bytes);
 }
 
 int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks) {
-  if (!b || !b->engine || !blocks) return fail(PDOSGPU_EINVAL, "NULL argument");
+  PDOS_TRY(ready(b));
+  if (!blocks) return fail(PDOSGPU_EINVAL, "NULL argument");
   return b->engine->set_blocks(blocks);
 }
 
@@ -1463,7 +1641,8 @@ int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m
 }
 
 int pdosgpu_batch_classes(pdosgpu_batch *b, int32_t *cls) {
-  if (!b || !b->engine || !cls) return fail(PDOSGPU_EINVAL, "NULL batch or output");
+  PDOS_TRY(ready(b));
+  if (!cls) return fail(PDOSGPU_EINVAL, "NULL output");
   for (int64_t i = 0; i < b->engine->count; ++i) cls[i] = b->engine->instance_class(i);
   return PDOSGPU_OK;
 }

@@ -9,6 +9,7 @@
 * ``pdos_call`` goes through the reference-compatible ``pdos()`` entry point.
 """
 import ctypes
+import time
 
 import numpy as np
 
@@ -175,17 +176,57 @@ class Batch:
 
     def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0):
         self.lib = _lib.load()
-        self.probs = list(probs)
-        self._keep = []
-        arr = _c_problems(self.probs, self._keep)
-        self._keep.append(arr)
+        probs = list(probs)
+        self.probs = probs
+        self.sizes = [(p.n, p.m) for p in probs]
+        keep = []
+        arr = _c_problems(probs, keep)
         self._opt = make_options(precision, "2norm", device)
         self._b = ctypes.c_void_p()
-        _lib.check(self.lib.pdosgpu_batch_setup(arr, len(self.probs), ctypes.byref(self._opt),
+        _lib.check(self.lib.pdosgpu_batch_setup(arr, len(probs), ctypes.byref(self._opt),
                                                 int(iters_per_launch), ctypes.byref(self._b)),
                    "pdosgpu_batch_setup", self.lib)
-        self.n_total = sum(p.n for p in self.probs)
-        self.m_total = sum(p.m for p in self.probs)
+        self._totals()
+
+    @classmethod
+    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0):
+        """A batch set up from an iterable of problem lists, one
+        pdosgpu_batch_append per list, so that only one list has to exist on
+        the host at a time (pdosgpu_batch_create / append / commit).  Keeps
+        the instances' sizes, not the problems."""
+        self = cls.__new__(cls)
+        self.lib = _lib.load()
+        self.probs = None
+        self.sizes = []
+        self._opt = make_options(precision, "2norm", device)
+        self._b = ctypes.c_void_p()
+        _lib.check(self.lib.pdosgpu_batch_create(ctypes.byref(self._opt), int(iters_per_launch),
+                                                 ctypes.byref(self._b)), "pdosgpu_batch_create", self.lib)
+        self.append_seconds = 0.0  # time inside the append calls (host arrays -> device layouts)
+        try:
+            for wave in waves:
+                wave = list(wave)
+                keep = []
+                arr = _c_problems(wave, keep)
+                t0 = time.perf_counter()
+                _lib.check(self.lib.pdosgpu_batch_append(self._b, arr, len(wave)), "pdosgpu_batch_append",
+                           self.lib)
+                self.append_seconds += time.perf_counter() - t0
+                self.sizes += [(p.n, p.m) for p in wave]
+                del keep, arr, wave
+            t0 = time.perf_counter()
+            _lib.check(self.lib.pdosgpu_batch_commit(self._b), "pdosgpu_batch_commit", self.lib)
+            self.commit_seconds = time.perf_counter() - t0
+        except Exception:
+            self.close()
+            raise
+        self._totals()
+        return self
+
+    def _totals(self):
+        self.count = len(self.sizes)
+        self.n_total = sum(n for n, _ in self.sizes)
+        self.m_total = sum(m for _, m in self.sizes)
 
     def solve(self):
         _lib.check(self.lib.pdosgpu_batch_solve(self._b), "pdosgpu_batch_solve", self.lib)
@@ -213,7 +254,7 @@ class Batch:
     def classes(self):
         """Size class of each instance: 0-3 by nonzeros, 4 = vectors staged in
         global memory (too large for one CTA's shared memory)."""
-        out = (ctypes.c_int32 * len(self.probs))()
+        out = (ctypes.c_int32 * self.count)()
         _lib.check(self.lib.pdosgpu_batch_classes(self._b, out), "pdosgpu_batch_classes", self.lib)
         return list(out)
 
@@ -243,7 +284,7 @@ class Batch:
 
     def infos(self):
         """Per-instance info dicts only (no solution vectors)."""
-        cnt = len(self.probs)
+        cnt = self.count
         infos = (_lib.Info * cnt)()
         dp = ctypes.POINTER(ctypes.c_double)
         _lib.check(self.lib.pdosgpu_batch_fetch(self._b, 0, cnt, dp(), dp(), dp(), infos),
@@ -257,7 +298,7 @@ class Batch:
 
     def fetch_all(self):
         """Stacked x, s, y and a list of per-instance info dicts."""
-        cnt = len(self.probs)
+        cnt = self.count
         x, s, y = np.zeros(self.n_total), np.zeros(self.m_total), np.zeros(self.m_total)
         infos = (_lib.Info * cnt)()
         dp = ctypes.POINTER(ctypes.c_double)
@@ -275,13 +316,13 @@ class Batch:
         """One result dict per instance, as Workspace.fetch returns."""
         x, s, y, infos = self.fetch_all()
         res, c0, r0 = [], 0, 0
-        for p, d in zip(self.probs, infos):
-            res.append({"x": x[c0:c0 + p.n].copy(), "s": s[r0:r0 + p.m].copy(),
-                        "y": y[r0:r0 + p.m].copy(),
+        for (n, m), d in zip(self.sizes, infos):
+            res.append({"x": x[c0:c0 + n].copy(), "s": s[r0:r0 + m].copy(),
+                        "y": y[r0:r0 + m].copy(),
                         "status": "Solved" if d["solved"] else "Indeterminate",
                         "iters": d["admm_iters"], "cg_iters": d["cg_iters"], "info": d})
-            c0 += p.n
-            r0 += p.m
+            c0 += n
+            r0 += m
         return res
 
     def close(self):

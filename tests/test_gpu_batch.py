@@ -243,3 +243,47 @@ def test_batch_rejects_what_it_cannot_run(built_lib, torch_cuda):
     # the GPU stays usable
     with Batch([a]) as ok:
         assert ok.solve().fetch()[0]["status"] in ("Solved", "Indeterminate")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batch_set_up_in_waves_is_bit_identical_to_one_call(built_lib, torch_cuda, precision):
+    """pdosgpu_batch_create / append / commit: the same instances appended in
+    three calls (three set-up waves, each with its own layout allocation)
+    give the same bits as one pdosgpu_batch_setup call, in every size class
+    and in the global staging class."""
+    from pdos_gb300.solver import Batch
+    probs = _uneven_portfolios() + _oversize_batch()
+    with Batch(probs, precision=precision) as one:
+        cls_one = one.classes()
+        x1, s1, y1, inf1 = one.solve().fetch_all()
+    waves = [probs[:3], probs[3:5], probs[5:]]
+    with Batch.in_waves(waves, precision=precision) as three:
+        cls_three = three.classes()
+        x3, s3, y3, inf3 = three.solve().fetch_all()
+    assert cls_one == cls_three and 4 in cls_one
+    assert np.array_equal(x1, x3) and np.array_equal(s1, s3) and np.array_equal(y1, y3)
+    assert [d["admm_iters"] for d in inf1] == [d["admm_iters"] for d in inf3]
+    assert [d["cg_iters"] for d in inf1] == [d["cg_iters"] for d in inf3]
+
+
+def test_batch_rejects_use_before_commit_and_append_after(built_lib, torch_cuda):
+    import ctypes
+    from pdos_gb300 import _lib
+    from pdos_gb300.solver import _c_problems, make_options
+    probs = _uneven_portfolios()[:2]
+    lib = built_lib
+    opt = make_options("fp32")
+    b = ctypes.c_void_p()
+    _lib.check(lib.pdosgpu_batch_create(ctypes.byref(opt), 0, ctypes.byref(b)), "create", lib)
+    try:
+        assert lib.pdosgpu_batch_solve(b) == _lib.PDOSGPU_EINVAL
+        assert "not committed" in _lib.last_error(lib)
+        assert lib.pdosgpu_batch_commit(b) == _lib.PDOSGPU_EINVAL  # nothing appended
+        keep = []
+        arr = _c_problems(probs, keep)
+        _lib.check(lib.pdosgpu_batch_append(b, arr, len(probs)), "append", lib)
+        _lib.check(lib.pdosgpu_batch_commit(b), "commit", lib)
+        assert lib.pdosgpu_batch_append(b, arr, len(probs)) == _lib.PDOSGPU_EINVAL
+        _lib.check(lib.pdosgpu_batch_solve(b), "solve", lib)
+    finally:
+        lib.pdosgpu_batch_free(b)

@@ -74,7 +74,7 @@ def test_family_batch_warm_start_matches_fp64_oracle(built_lib, torch_cuda, fami
     fam, params = family_case["fam"], family_case["params"]
     tmus, tds = fam.draw(1024, seed=11)
     X, Y, S, _ = solve_family(fam, tmus, tds, dict(params, EPS_ABS=1e-5), "fp32")
-    ws = FamilyWarmStart(fam, hidden=256, max_batch=len(family_case["probs"]), seed=0)
+    ws = FamilyWarmStart(fam, hidden=256, max_batch=128, seed=0)  # training batches of 128
     try:
         ws.fit(tmus, tds, X, Y, S, epochs=20, batch=128, lr=1e-3)
         probs = family_case["probs"]
