@@ -27,6 +27,7 @@ enum {
 
 enum { PDOSGPU_FP64 = 0, PDOSGPU_FP32 = 1 };          /* storage/arithmetic */
 enum { PDOSGPU_SCALE_2NORM = 0, PDOSGPU_SCALE_RUIZ = 1 }; /* NORMALIZE=1 kind */
+enum { PDOSGPU_BATCH_SHARE = 0, PDOSGPU_BATCH_OWN = 1 };  /* batch layouts */
 
 typedef struct {
   int precision;   /* PDOSGPU_FP64 (default): every operation in double, the
@@ -37,7 +38,14 @@ typedef struct {
                       (common.h:69-162, the reference's default build) or
                       PDOSGPU_SCALE_RUIZ (ruiz_equil_common.h:98-322) */
   int device;      /* CUDA device ordinal (default 0) */
-  int reserved[5];
+  int batch_layouts; /* batches only: PDOSGPU_BATCH_SHARE (default) lets the
+                        instances of a family -- one sparsity pattern, cone
+                        table and sizes, values differing at no more than a
+                        quarter of the nonzeros, NORMALIZE=0 -- share one
+                        matrix layout, each keeping only its own values of
+                        the entries that differ (same results, bit for bit);
+                        PDOSGPU_BATCH_OWN gives every instance its own */
+  int reserved[4];
 } pdosgpu_options;
 
 typedef struct {
@@ -189,6 +197,11 @@ int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks);
 /* Number of instances and stacked sizes (any may be NULL). */
 int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m,
                         int64_t *nnz);
+/* Matrix layouts of the batch (any output may be NULL): family groups
+ * sharing one layout, instances on shared layouts, and the device bytes of
+ * every layout (tables, indices, values, the group members' own values). */
+int pdosgpu_batch_layouts(pdosgpu_batch *b, int64_t *groups, int64_t *instances,
+                          int64_t *bytes);
 /* Size class of every instance (cls[count]): 0-3 by nonzeros (at most
  * 4,096 / 32,768 / 262,144 / more), vectors staged in shared memory; 4:
  * too large for shared memory, vectors staged in global memory. */

@@ -23,11 +23,13 @@ PDOSGPU_FP64 = 0
 PDOSGPU_FP32 = 1
 PDOSGPU_SCALE_2NORM = 0
 PDOSGPU_SCALE_RUIZ = 1
+PDOSGPU_BATCH_SHARE = 0
+PDOSGPU_BATCH_OWN = 1
 
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("scaling", c_int), ("device", c_int),
-                ("reserved", c_int * 5)]
+                ("batch_layouts", c_int), ("reserved", c_int * 4)]
 
 
 class Info(ctypes.Structure):
@@ -93,6 +95,7 @@ SIGNATURES = {
     "pdosgpu_batch_fetch": (c_int, [c_void_p, c_int64, c_int64, _D, _D, _D, POINTER(Info)]),
     "pdosgpu_batch_done": (c_int64, [c_void_p]),
     "pdosgpu_batch_classes": (c_int, [c_void_p, c_void_p]),
+    "pdosgpu_batch_layouts": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
     "pdosgpu_batch_tune": (c_int, [c_void_p, c_int, POINTER(c_int)]),
     "pdosgpu_batch_set_blocks": (c_int, [c_void_p, POINTER(c_int)]),
     "pdosgpu_batch_time_products": (c_int, [c_void_p, c_int, POINTER(c_double), POINTER(c_double)]),

@@ -77,7 +77,12 @@ struct Inst {
   Side A, At;
   double lambda, pscale, dscale, alpha, eps, tol_sq;
   int64_t max_iters, cg_max;
-  HybPtr hA, hT;  // layout arrays of the instance's wave
+  HybPtr hA, hT;  // layout arrays of the instance's wave (or of its family group)
+  // Family groups (instances with one pattern whose values differ only at
+  // a few positions) share hA / hT; the shared value arrays then hold, at
+  // each position that varies within the group, a NaN whose payload indexes
+  // the instance's own values here (layout order).  nullptr: own layout.
+  const void *pvA, *pvT;
 };
 
 struct State {
@@ -198,6 +203,25 @@ __device__ __forceinline__ Val4<double> ld_stream4(const double *p) {
   return r;
 }
 
+// Varying entries of a shared (family) layout: the shared value array holds
+// a quiet NaN whose low 22 bits index the instance's own value of that
+// entry.  Input data is checked finite at set-up, so no genuine value is a
+// NaN.
+constexpr uint32_t kBoxBits = 22;
+__host__ __device__ __forceinline__ bool box_index_fits(int64_t t) { return t >= 0 && t < ((int64_t)1 << kBoxBits); }
+__device__ __forceinline__ float nan_box(float, uint32_t t) { return __uint_as_float(0x7FC00000u | t); }
+__device__ __forceinline__ double nan_box(double, uint32_t t) {
+  return __longlong_as_double((long long)(0x7FF8000000000000ull | (unsigned long long)t));
+}
+__device__ __forceinline__ uint32_t box_payload(float v) { return __float_as_uint(v) & ((1u << kBoxBits) - 1); }
+__device__ __forceinline__ uint32_t box_payload(double v) {
+  return (uint32_t)((unsigned long long)__double_as_longlong(v) & ((1ull << kBoxBits) - 1));
+}
+template <typename T>
+__device__ __forceinline__ T unbox(T v, const T *pv) {
+  return v != v ? __ldg(pv + box_payload(v)) : v;
+}
+
 // Four consecutive entries of one row into the NV running sums, in order.
 template <typename T, int NV>
 __device__ __forceinline__ void fma4(const Idx4 &j, const Val4<T> &v, const T *src0, const T *src1,
@@ -220,9 +244,11 @@ __device__ __forceinline__ void fma4(const Idx4 &j, const Val4<T> &v, const T *s
 // every 128); slices of width >= 4 are stored four columns at a time per
 // lane ([c/4][lane][c%4]), narrower ones one column at a time ([c][lane]).
 // Split rows leave piece partials in pbuf and are finished after a barrier.
-template <typename T, int BLOCK, int NV, class Epi>
-__device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, const T *src0,
-                                            const T *src1, T *pbuf, Epi &&epi) {
+// SHARED: the layout is a family group's; pv holds this instance's values
+// of the entries that vary within the group (see unbox).
+template <typename T, int BLOCK, int NV, bool SHARED, class Epi>
+__device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd, const T *pv, const T *src0,
+                                                 const T *src1, T *pbuf, Epi &&epi) {
   constexpr int W = BLOCK / 32;
   const T *const hval = static_cast<const T *>(H.val);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -237,7 +263,8 @@ __device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, con
 #pragma unroll kUnroll
     for (int e = 4 * lane; e < len; e += 128) {
       const Idx4 j = ld_stream4(ip + e);
-      const Val4<T> v = ld_stream4(vp + e);
+      Val4<T> v = ld_stream4(vp + e);
+      if (SHARED) v = Val4<T>{unbox(v.x, pv), unbox(v.y, pv), unbox(v.z, pv), unbox(v.w, pv)};
       fma4<T, NV>(j, v, src0, src1, a0, a1);
     }
     a0 = warp_sum_t(a0);
@@ -262,7 +289,8 @@ __device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, con
 #pragma unroll kUnroll
       for (int c4 = 0; c4 < -width; c4 += 4) {
         const Idx4 j = ld_stream4(ip + 32 * c4);
-        const Val4<T> v = ld_stream4(vp + 32 * c4);
+        Val4<T> v = ld_stream4(vp + 32 * c4);
+        if (SHARED) v = Val4<T>{unbox(v.x, pv), unbox(v.y, pv), unbox(v.z, pv), unbox(v.w, pv)};
         fma4<T, NV>(j, v, src0, src1, a0, a1);
       }
     } else {
@@ -270,7 +298,8 @@ __device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, con
       const T *vp = hval + off + lane;
       for (int c = 0; c < width; ++c) {
         const int j = ip[c * 32];
-        const T v = vp[c * 32];
+        T v = vp[c * 32];
+        if (SHARED) v = unbox(v, pv);
         a0 = fma(v, src0[j], a0);
         if (NV == 2) a1 = fma(v, src1[j], a1);
       }
@@ -290,6 +319,17 @@ __device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, con
       epi(H.split_row[sk], a0, a1);
     }
   }
+}
+
+// One product over one side of an instance, through its own layout or its
+// family group's shared one.
+template <typename T, int BLOCK, int NV, class Epi>
+__device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, const void *pv, const T *src0,
+                                            const T *src1, T *pbuf, Epi &&epi) {
+  if (pv)
+    hyb_product_impl<T, BLOCK, NV, true>(H, sd, static_cast<const T *>(pv), src0, src1, pbuf, epi);
+  else
+    hyb_product_impl<T, BLOCK, NV, false>(H, sd, nullptr, src0, src1, pbuf, epi);
 }
 
 // Three-case SOC rule of cones.c:21-47 for one element.
@@ -341,7 +381,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     double red[2] = {0.0, 0.0};
-    hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int r, T a, T) {
+    hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int r, T a, T) {
       ax[r] = a;
       const T sv = s[r], bv = b[r], yv = y[r];
       const T pr = ((sv - bv) + a) / D[r];
@@ -364,7 +404,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     }
     __syncthreads();
     double top[3] = {0.0, 0.0, 0.0};
-    hyb_product<T, BLOCK, 2>(I.hT, I.At, g1, g2, pbuf, [&](int j, T sy, T su) {
+    hyb_product<T, BLOCK, 2>(I.hT, I.At, I.pvT, g1, g2, pbuf, [&](int j, T sy, T su) {
       const T cj = c[j];
       const T dr = (cj + sy) / E[j];
       top[0] += (double)dr * (double)dr;
@@ -395,10 +435,10 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       __syncthreads();
     }
     while (active) {
-      hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int r, T a, T) { g2[r] = a; });
+      hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int r, T a, T) { g2[r] = a; });
       __syncthreads();
       double pt[1] = {0.0};
-      hyb_product<T, BLOCK, 1>(I.hT, I.At, g2, g2, pbuf, [&](int j, T a, T) {
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, g2, g2, pbuf, [&](int j, T a, T) {
         const T pj = g1[j];
         const T tj = pj + a;
         tt[j] = tj;
@@ -437,7 +477,7 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     double fin[2] = {0.0, 0.0};
-    hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int r, T a, T) {
+    hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int r, T a, T) {
       T stv = b[r] + (-a);
       stv = alpha * stv + oma * s[r];
       T v = stv - lam * y[r];
@@ -563,9 +603,9 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev
     for (int j = threadIdx.x; j < I.n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     for (int r = 0; r < reps; ++r) {
-      hyb_product<T, BLOCK, 1>(I.hA, I.A, g1, g1, pbuf, [&](int row, T a, T) { g2[row] = a; });
+      hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int row, T a, T) { g2[row] = a; });
       __syncthreads();
-      hyb_product<T, BLOCK, 1>(I.hT, I.At, g2, g2, pbuf, [&](int j, T a, T) { tt[j] = g1[j] + a; });
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, g2, g2, pbuf, [&](int j, T a, T) { tt[j] = g1[j] + a; });
       __syncthreads();
     }
   }
@@ -608,20 +648,36 @@ __global__ void warm_start_kernel(const double *x0, const double *y0, const doub
   }
 }
 
+// Layout values from their source positions: p >= 0 the value at p, -1
+// padding (zero), p <= -2 the varying entry -2 - p of a family group (its
+// NaN box).
 template <typename T>
 __global__ void gather_values_kernel(const int32_t *src, int64_t count, const T *from, T *to) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t p = src[i];
-    to[i] = p >= 0 ? from[p] : T(0);
+    to[i] = p >= 0 ? from[p] : (p == -1 ? T(0) : nan_box(T(0), (uint32_t)(-2 - p)));
   }
+}
+
+// Values at 64-bit source positions (the varying entries of a family group's
+// instances in the wave's stacked arrays).
+template <typename T>
+__global__ void gather_values64_kernel(const int64_t *src, int64_t count, const T *from, T *to) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    to[i] = from[src[i]];
 }
 
 // ------------------------------------------------------------ host side
 // Uploads one side's layout of one wave; values are gathered on the device
 // from the wave's (scaled) value array through the layout's source map.
 template <typename T>
-int upload_hyb(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStream_t st, HybPtr &h) {
+int upload_hyb(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStream_t st, HybPtr &h,
+               int64_t *bytes) {
+  *bytes += (int64_t)(hb.slice_beg.size() * 8 + hb.slice_w.size() * 4 + hb.slice_skip.size() * 4 +
+                      hb.piece_row.size() * 4 + hb.piece_beg.size() * 8 + hb.piece_len.size() * 4 +
+                      hb.split_row.size() * 12 + hb.idx.size() * 2 + hb.src.size() * sizeof(T));
   auto up = [&](auto **dst, const auto &v) -> int {
     using E = typename std::decay_t<decltype(v)>::value_type;
     E *p = nullptr;
@@ -695,6 +751,89 @@ KernelOf<T> products_kernel_for(int block, bool global) {
   }
 }
 
+// Instances of one wave that share a pattern (sizes, cone table, Ap, Ai)
+// and whose values differ only at a few positions: `vary` marks, per CSC
+// position, where any member's value differs from the first member's.
+struct FamilyGroup {
+  std::vector<int64_t> members;
+  std::vector<uint8_t> vary;
+  int64_t nvary = 0;
+};
+
+// 64-bit mix of the words of a problem's pattern (a filter; equality is
+// checked exactly afterwards).
+inline uint64_t pattern_hash(const pdosgpu_problem &p) {
+  uint64_t h = 0x9E3779B97F4A7C15ull;
+  auto mix = [&](uint64_t v) {
+    h ^= v + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h *= 0xBF58476D1CE4E5B9ull;
+  };
+  mix((uint64_t)p.m);
+  mix((uint64_t)p.n);
+  mix((uint64_t)p.f);
+  mix((uint64_t)p.l);
+  mix((uint64_t)p.qsize);
+  for (int64_t k = 0; k < p.qsize; ++k) mix((uint64_t)p.q[k]);
+  for (int64_t j = 0; j <= p.n; ++j) mix((uint64_t)p.Ap[j]);
+  const int64_t nz = p.Ap[p.n];
+  for (int64_t k = 0; k < nz; ++k) mix((uint64_t)p.Ai[k]);
+  return h;
+}
+
+inline bool same_pattern(const pdosgpu_problem &a, const pdosgpu_problem &b) {
+  if (a.m != b.m || a.n != b.n || a.f != b.f || a.l != b.l || a.qsize != b.qsize) return false;
+  if (a.qsize > 0 && std::memcmp(a.q, b.q, sizeof(int64_t) * a.qsize) != 0) return false;
+  if (std::memcmp(a.Ap, b.Ap, sizeof(int64_t) * (a.n + 1)) != 0) return false;
+  const int64_t nz = a.Ap[a.n];
+  return nz == 0 || std::memcmp(a.Ai, b.Ai, sizeof(int64_t) * nz) == 0;
+}
+
+// Family groups of at least two instances whose varying positions are at
+// most a quarter of the nonzeros (and few enough for the NaN boxes).
+inline std::vector<FamilyGroup> find_family_groups(const pdosgpu_problem *probs, int64_t cnt) {
+  std::vector<FamilyGroup> out;
+  if (cnt < 2) return out;
+  std::vector<uint64_t> key(cnt);
+  parallel_for(cnt, [&](int64_t i) { key[i] = pattern_hash(probs[i]); });
+  std::vector<int64_t> order(cnt);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
+  std::vector<std::vector<int64_t>> cand;
+  for (int64_t s0 = 0; s0 < cnt;) {
+    int64_t s1 = s0 + 1;
+    while (s1 < cnt && key[order[s1]] == key[order[s0]]) ++s1;
+    if (s1 - s0 >= 2) {
+      std::vector<int64_t> mem(order.begin() + s0, order.begin() + s1);
+      std::sort(mem.begin(), mem.end());
+      cand.push_back(std::move(mem));
+    }
+    s0 = s1;
+  }
+  for (auto &mem : cand) {
+    const pdosgpu_problem &r = probs[mem[0]];
+    std::vector<uint8_t> same(mem.size(), 1);
+    parallel_for((int64_t)mem.size(), [&](int64_t k) { same[k] = same_pattern(r, probs[mem[k]]) ? 1 : 0; });
+    FamilyGroup fg;
+    for (size_t k = 0; k < mem.size(); ++k)
+      if (same[k]) fg.members.push_back(mem[k]);
+    if (fg.members.size() < 2) continue;
+    const int64_t nz = r.Ap[r.n];
+    fg.vary.assign(nz > 0 ? nz : 1, 0);
+    const int64_t chunk = 4096, nchunks = (nz + chunk - 1) / chunk;
+    parallel_for(nchunks, [&](int64_t c) {
+      const int64_t k0 = c * chunk, k1 = std::min(nz, k0 + chunk);
+      for (size_t k = 1; k < fg.members.size(); ++k) {
+        const double *a = probs[fg.members[k]].Ax;
+        for (int64_t e = k0; e < k1; ++e)
+          if (a[e] != r.Ax[e]) fg.vary[e] = 1;
+      }
+    });
+    for (int64_t e = 0; e < nz; ++e) fg.nvary += fg.vary[e];
+    if (fg.nvary * 4 <= nz && box_index_fits(fg.nvary)) out.push_back(std::move(fg));
+  }
+  return out;
+}
+
 class BatchBase {
  public:
   virtual ~BatchBase() {}
@@ -713,6 +852,8 @@ class BatchBase {
   virtual int64_t done_count() = 0;
   bool committed = false;
   int64_t count = 0, total_n = 0, total_m = 0, total_nnz = 0, waves = 0;
+  int64_t family_groups = 0, family_instances = 0;  // instances on shared layouts
+  int64_t layout_bytes = 0;                          // device bytes of every layout
   double setup_ms = 0, solve_ms = 0;
   int64_t launches = 0;
   std::vector<int64_t> row0{0}, col0{0};
@@ -832,6 +973,8 @@ int BatchEngine<T>::append(const pdosgpu_problem *probs, int64_t cnt) {
   }
   if (normalize_ && opt_.scaling == PDOSGPU_SCALE_RUIZ)
     return fail(PDOSGPU_ENOTSUP, "Ruiz equilibration is not available for batches");
+  if (opt_.batch_layouts != PDOSGPU_BATCH_SHARE && opt_.batch_layouts != PDOSGPU_BATCH_OWN)
+    return fail(PDOSGPU_EINVAL, "batch_layouts must be PDOSGPU_BATCH_SHARE or PDOSGPU_BATCH_OWN");
   PDOS_CUDA_TRY(cudaSetDevice(opt_.device));
   size_t free_b = 0, total_b = 0;
   PDOS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -1006,37 +1149,149 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
     col0.push_back(I.col0 + p.n);
   }
   auto arena = std::make_unique<DeviceArena>();
-  {
+  const int32_t *rp = P.rp_host.data(), *ap = P.ap_host.data();
+  const int32_t *rj = Rj.data();
+  const int64_t *ai = Ai.data();
+  // ---- family groups share one layout (NORMALIZE = 0 only: scaling would
+  // give every instance its own values)
+  std::vector<FamilyGroup> groups;
+  std::vector<int32_t> group_of(cnt, -1);
+  if (!normalize_ && opt_.batch_layouts == PDOSGPU_BATCH_SHARE) groups = find_family_groups(probs, cnt);
+  for (size_t g = 0; g < groups.size(); ++g)
+    for (int64_t i : groups[g].members) group_of[i] = (int32_t)g;
+  {  // instances with their own layout
+    std::vector<int64_t> own;
+    for (int64_t i = 0; i < cnt; ++i)
+      if (group_of[i] < 0) own.push_back(i);
+    if (!own.empty()) {
+      HybBuild bA, bT;
+      std::vector<Side> sides;
+      const int64_t no = (int64_t)own.size();
+      build_layout<int32_t>(bA, no, [&](int64_t k, const int32_t *&ptr, const int32_t *&g, int64_t &r0,
+                                        int64_t &r1, int64_t &c0) {
+        const int64_t i = own[k];
+        ptr = rp;
+        g = rj;
+        r0 = wrow0[i];
+        r1 = wrow0[i + 1];
+        c0 = wcol0[i];
+      }, sides);
+      for (int64_t k = 0; k < no; ++k) inst_h_[first + own[k]].A = sides[k];
+      build_layout<int64_t>(bT, no, [&](int64_t k, const int32_t *&ptr, const int64_t *&g, int64_t &r0,
+                                        int64_t &r1, int64_t &c0) {
+        const int64_t i = own[k];
+        ptr = ap;
+        g = ai;
+        r0 = wcol0[i];
+        r1 = wcol0[i + 1];
+        c0 = wrow0[i];
+      }, sides);
+      for (int64_t k = 0; k < no; ++k) inst_h_[first + own[k]].At = sides[k];
+      HybPtr hA{}, hT{};
+      PDOS_TRY(upload_hyb<T>(bA, P.Rx, *arena, st, hA, &layout_bytes));
+      PDOS_TRY(upload_hyb<T>(bT, P.Ax, *arena, st, hT, &layout_bytes));
+      for (int64_t k = 0; k < no; ++k) {
+        inst_h_[first + own[k]].hA = hA;
+        inst_h_[first + own[k]].hT = hT;
+      }
+    }
+  }
+  for (const FamilyGroup &fg : groups) {  // one layout per group, built from its first member
+    const int64_t ref = fg.members[0];
+    const pdosgpu_problem &pr = probs[ref];
+    const int64_t nz = pr.Ap[pr.n];
+    // CSR position -> CSC position within the instance (the stable
+    // transpose, cs.c:146-168)
+    std::vector<int64_t> csr2csc(nz > 0 ? nz : 1), next(pr.m + 1, 0);
+    for (int64_t k = 0; k < nz; ++k) ++next[pr.Ai[k] + 1];
+    for (int64_t r = 0; r < pr.m; ++r) next[r + 1] += next[r];
+    for (int64_t j = 0; j < pr.n; ++j)
+      for (int64_t k = pr.Ap[j]; k < pr.Ap[j + 1]; ++k) csr2csc[next[pr.Ai[k]]++] = k;
+    const int64_t rbase = rp[wrow0[ref]], cbase = Ap[wcol0[ref]];
     HybBuild bA, bT;
-    std::vector<Side> sides;
-    const int32_t *rp = P.rp_host.data(), *ap = P.ap_host.data();
-    const int32_t *rj = Rj.data();
-    const int64_t *ai = Ai.data();
-    build_layout<int32_t>(bA, cnt, [&](int64_t i, const int32_t *&ptr, const int32_t *&g, int64_t &r0,
-                                       int64_t &r1, int64_t &c0) {
+    std::vector<Side> sA, sT;
+    build_layout<int32_t>(bA, 1, [&](int64_t, const int32_t *&ptr, const int32_t *&g, int64_t &r0, int64_t &r1,
+                                     int64_t &c0) {
       ptr = rp;
       g = rj;
-      r0 = wrow0[i];
-      r1 = wrow0[i + 1];
-      c0 = wcol0[i];
-    }, sides);
-    for (int64_t i = 0; i < cnt; ++i) inst_h_[first + i].A = sides[i];
-    build_layout<int64_t>(bT, cnt, [&](int64_t i, const int32_t *&ptr, const int64_t *&g, int64_t &r0,
-                                       int64_t &r1, int64_t &c0) {
+      r0 = wrow0[ref];
+      r1 = wrow0[ref + 1];
+      c0 = wcol0[ref];
+    }, sA);
+    build_layout<int64_t>(bT, 1, [&](int64_t, const int32_t *&ptr, const int64_t *&g, int64_t &r0, int64_t &r1,
+                                     int64_t &c0) {
       ptr = ap;
       g = ai;
-      r0 = wcol0[i];
-      r1 = wcol0[i + 1];
-      c0 = wrow0[i];
-    }, sides);
-    for (int64_t i = 0; i < cnt; ++i) inst_h_[first + i].At = sides[i];
-    HybPtr hA{}, hT{};
-    PDOS_TRY(upload_hyb<T>(bA, P.Rx, *arena, st, hA));
-    PDOS_TRY(upload_hyb<T>(bT, P.Ax, *arena, st, hT));
-    for (int64_t i = 0; i < cnt; ++i) {
-      inst_h_[first + i].hA = hA;
-      inst_h_[first + i].hT = hT;
+      r0 = wcol0[ref];
+      r1 = wcol0[ref + 1];
+      c0 = wrow0[ref];
+    }, sT);
+    // varying entries become NaN boxes numbered in layout order; vpos keeps
+    // each one's position within the instance (CSR for A, CSC for A')
+    std::vector<int64_t> vposA, vposT;
+    for (size_t e = 0; e < bA.src.size(); ++e) {
+      const int32_t p = bA.src[e];
+      if (p < 0) continue;
+      const int64_t local = p - rbase;
+      if (fg.vary[csr2csc[local]]) {
+        bA.src[e] = -2 - (int32_t)vposA.size();
+        vposA.push_back(local);
+      }
     }
+    for (size_t e = 0; e < bT.src.size(); ++e) {
+      const int32_t p = bT.src[e];
+      if (p < 0) continue;
+      const int64_t local = p - cbase;
+      if (fg.vary[local]) {
+        bT.src[e] = -2 - (int32_t)vposT.size();
+        vposT.push_back(local);
+      }
+    }
+    HybPtr hA{}, hT{};
+    PDOS_TRY(upload_hyb<T>(bA, P.Rx, *arena, st, hA, &layout_bytes));
+    PDOS_TRY(upload_hyb<T>(bT, P.Ax, *arena, st, hT, &layout_bytes));
+    // every member's values of the varying entries, in layout order
+    const int64_t nm = (int64_t)fg.members.size(), na = (int64_t)vposA.size(), nt = (int64_t)vposT.size();
+    T *pvA = nullptr, *pvT = nullptr;
+    PDOS_TRY(arena->alloc(&pvA, (size_t)(nm * na)));
+    PDOS_TRY(arena->alloc(&pvT, (size_t)(nm * nt)));
+    layout_bytes += (nm * na + nm * nt) * (int64_t)sizeof(T);
+    {
+      std::vector<int64_t> srcA((size_t)(nm * na)), srcT((size_t)(nm * nt));
+      for (int64_t k = 0; k < nm; ++k) {
+        const int64_t i = fg.members[k];
+        const int64_t rb = rp[wrow0[i]], cb = Ap[wcol0[i]];
+        for (int64_t t = 0; t < na; ++t) srcA[k * na + t] = rb + vposA[t];
+        for (int64_t t = 0; t < nt; ++t) srcT[k * nt + t] = cb + vposT[t];
+      }
+      DeviceArena tmp;
+      int64_t *dA = nullptr, *dT = nullptr;
+      PDOS_TRY(tmp.alloc(&dA, srcA.size()));
+      PDOS_TRY(tmp.alloc(&dT, srcT.size()));
+      if (!srcA.empty()) {
+        PDOS_CUDA_TRY(cudaMemcpyAsync(dA, srcA.data(), sizeof(int64_t) * srcA.size(), cudaMemcpyHostToDevice, st));
+        const int g = (int)std::min<int64_t>(((int64_t)srcA.size() + 255) / 256, (int64_t)num_sms() * 16);
+        gather_values64_kernel<T><<<g, 256, 0, st>>>(dA, (int64_t)srcA.size(), P.Rx, pvA);
+      }
+      if (!srcT.empty()) {
+        PDOS_CUDA_TRY(cudaMemcpyAsync(dT, srcT.data(), sizeof(int64_t) * srcT.size(), cudaMemcpyHostToDevice, st));
+        const int g = (int)std::min<int64_t>(((int64_t)srcT.size() + 255) / 256, (int64_t)num_sms() * 16);
+        gather_values64_kernel<T><<<g, 256, 0, st>>>(dT, (int64_t)srcT.size(), P.Ax, pvT);
+      }
+      PDOS_CUDA_TRY(cudaGetLastError());
+      PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before the host and temporary arrays go
+    }
+    for (int64_t k = 0; k < nm; ++k) {
+      Inst &I = inst_h_[first + fg.members[k]];
+      I.A = sA[0];
+      I.At = sT[0];
+      I.hA = hA;
+      I.hT = hT;
+      I.pvA = pvA + k * na;
+      I.pvT = pvT + k * nt;
+    }
+    ++family_groups;
+    family_instances += nm;
   }
   // an instance whose own staging regions exceed one CTA's shared memory
   // goes to the global class
@@ -1637,6 +1892,14 @@ int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m
   if (n) *n = b->engine->total_n;
   if (m) *m = b->engine->total_m;
   if (nnz) *nnz = b->engine->total_nnz;
+  return PDOSGPU_OK;
+}
+
+int pdosgpu_batch_layouts(pdosgpu_batch *b, int64_t *groups, int64_t *instances, int64_t *bytes) {
+  if (!b || !b->engine) return fail(PDOSGPU_EINVAL, "NULL batch");
+  if (groups) *groups = b->engine->family_groups;
+  if (instances) *instances = b->engine->family_instances;
+  if (bytes) *bytes = b->engine->layout_bytes;
   return PDOSGPU_OK;
 }
 

@@ -21,7 +21,7 @@ _PRECISION = {"fp64": _lib.PDOSGPU_FP64, "fp32": _lib.PDOSGPU_FP32}
 _SCALING = {"2norm": _lib.PDOSGPU_SCALE_2NORM, "ruiz": _lib.PDOSGPU_SCALE_RUIZ}
 
 
-def make_options(precision="fp64", scaling="2norm", device=0):
+def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True):
     if precision not in _PRECISION:
         raise ValueError(f"precision must be one of {sorted(_PRECISION)}")
     if scaling not in _SCALING:
@@ -31,6 +31,7 @@ def make_options(precision="fp64", scaling="2norm", device=0):
     opt.precision = _PRECISION[precision]
     opt.scaling = _SCALING[scaling]
     opt.device = device
+    opt.batch_layouts = _lib.PDOSGPU_BATCH_SHARE if share_layouts else _lib.PDOSGPU_BATCH_OWN
     return opt
 
 
@@ -174,14 +175,14 @@ class Batch:
     """Many independent problems solved together (pdosgpu_batch_*): one CTA
     per instance at a time, convergence masking, per-instance results."""
 
-    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0):
+    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0, share_layouts=True):
         self.lib = _lib.load()
         probs = list(probs)
         self.probs = probs
         self.sizes = [(p.n, p.m) for p in probs]
         keep = []
         arr = _c_problems(probs, keep)
-        self._opt = make_options(precision, "2norm", device)
+        self._opt = make_options(precision, "2norm", device, share_layouts)
         self._b = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_batch_setup(arr, len(probs), ctypes.byref(self._opt),
                                                 int(iters_per_launch), ctypes.byref(self._b)),
@@ -189,7 +190,7 @@ class Batch:
         self._totals()
 
     @classmethod
-    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0):
+    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0, share_layouts=True):
         """A batch set up from an iterable of problem lists, one
         pdosgpu_batch_append per list, so that only one list has to exist on
         the host at a time (pdosgpu_batch_create / append / commit).  Keeps
@@ -198,7 +199,7 @@ class Batch:
         self.lib = _lib.load()
         self.probs = None
         self.sizes = []
-        self._opt = make_options(precision, "2norm", device)
+        self._opt = make_options(precision, "2norm", device, share_layouts)
         self._b = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_batch_create(ctypes.byref(self._opt), int(iters_per_launch),
                                                  ctypes.byref(self._b)), "pdosgpu_batch_create", self.lib)
@@ -257,6 +258,13 @@ class Batch:
         out = (ctypes.c_int32 * self.count)()
         _lib.check(self.lib.pdosgpu_batch_classes(self._b, out), "pdosgpu_batch_classes", self.lib)
         return list(out)
+
+    def layouts(self):
+        """(family groups, instances on shared layouts, device bytes of the layouts)."""
+        g, i, nb = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self.lib.pdosgpu_batch_layouts(self._b, ctypes.byref(g), ctypes.byref(i), ctypes.byref(nb)),
+                   "pdosgpu_batch_layouts", self.lib)
+        return g.value, i.value, nb.value
 
     def tune(self, iters=8):
         blocks = (ctypes.c_int * 5)()

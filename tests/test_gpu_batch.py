@@ -287,3 +287,45 @@ def test_batch_rejects_use_before_commit_and_append_after(built_lib, torch_cuda)
         _lib.check(lib.pdosgpu_batch_solve(b), "solve", lib)
     finally:
         lib.pdosgpu_batch_free(b)
+
+
+def _two_families_and_others():
+    """Two portfolio families (shared F; mu and D drawn per instance), their
+    members interleaved with unrelated instances."""
+    from pdos_gb300 import generators as g
+    P = dict(EPS_ABS=1e-4, VERBOSE=0, MAX_ITERS=3000)
+    fa = g.PortfolioFamily(300, 30, 0.2, seed=3)
+    fb = g.PortfolioFamily(1200, 60, 0.2, seed=4)
+    ma, da = fa.draw(12, seed=5)
+    mb, db = fb.draw(6, seed=6)
+    probs = []
+    for i in range(12):
+        probs.append(fa.instance(ma[i], da[i], P))
+        if i < 6:
+            probs.append(fb.instance(mb[i], db[i], P))
+        if i % 4 == 0:
+            probs.append(g.portfolio(100 + 10 * i, 10, 0.5, seed=90 + i, params=P))
+    return probs
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_family_groups_share_a_layout_with_identical_bits(built_lib, torch_cuda, precision):
+    """Instances of one family share one matrix layout and keep only their own
+    values of the entries that differ (the D^(1/2) entries); results are the
+    bits of the batch in which every instance has its own layout."""
+    from pdos_gb300.solver import Batch
+    probs = _two_families_and_others()
+    with Batch(probs, precision=precision, share_layouts=False) as own:
+        assert own.layouts()[:2] == (0, 0)
+        own_bytes = own.layouts()[2]
+        x1, s1, y1, inf1 = own.solve().fetch_all()
+    with Batch(probs, precision=precision) as shared:
+        groups, members, shared_bytes = shared.layouts()
+        x2, s2, y2, inf2 = shared.solve().fetch_all()
+        again = shared.reset().solve().fetch_all()
+    assert (groups, members) == (2, 18)
+    assert shared_bytes < 0.5 * own_bytes
+    assert np.array_equal(x1, x2) and np.array_equal(s1, s2) and np.array_equal(y1, y2)
+    assert [d["admm_iters"] for d in inf1] == [d["admm_iters"] for d in inf2]
+    assert np.array_equal(again[0], x2)
+    assert all(d["solved"] for d in inf2)
