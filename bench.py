@@ -230,6 +230,37 @@ def spmv_bytes(prob, which, sv):
     return nnz * (sv + 4) + m * sv + 2 * N * sv + 8 * N
 
 
+def single_instance_spmv(device, reps=20):
+    """The single-instance FP64 engine's SpMV kernels on the n = 200,000
+    portfolio (k = 2,000, F at 5 %: 20.6M nonzeros, A and A' 0.5 GB, far
+    above L2), timed with CUDA events on the workspace stream, against two
+    ceilings: the measured HBM copy rate and the device's FP64 FMA rate
+    (one FMA per nonzero), both expressed in GB/s of the kernel's
+    algorithmic bytes."""
+    from pdos_gb300.solver import Workspace, fp64_fma_rate
+    wl = WORKLOADS["portfolio_n200k_fp64"]
+    prob = make_problem(wl)
+    fma = fp64_fma_rate(device)
+    peak, peak_kind = measured_peaks()
+    out = {"workload": "portfolio_n200k_fp64", "nnz": prob.nnz, "n_vars": prob.n, "m_rows": prob.m,
+           "fp64_fma_per_s": fma, "hbm_peak_gbs": peak, "hbm_peak_kind": peak_kind}
+    with Workspace(prob, "fp64", device=device) as w:
+        for which, name in ((4, "u = A p"), (5, "t = p + A'u")):
+            ms = w.time_kernel(which, reps)
+            pass_ms = w.time_kernel(which - 4, reps)
+            nbytes = spmv_bytes(prob, which - 4, 8)
+            achieved = nbytes / (ms / 1e3) / 1e9
+            fp64_gbs = nbytes / (prob.nnz / fma) / 1e9
+            ceiling = min(peak, fp64_gbs)
+            out["sell_spmv_kernel<%s>" % ("OpCgA" if which == 4 else "OpCgAt")] = {
+                "product": name, "ms_per_launch": ms, "pass_ms_with_combine": pass_ms, "bytes_per_launch": nbytes,
+                "achieved_gbs": achieved, "frac_of_hbm": achieved / peak,
+                "fp64_fma_ceiling_gbs": fp64_gbs, "frac_of_fp64_fma_ceiling": achieved / fp64_gbs,
+                "frac_of_min_ceiling": achieved / ceiling,
+                "bound_by": "hbm" if peak <= fp64_gbs else "fp64 fma"}
+    return out
+
+
 def run_reference(args, wl, prob):
     """--impl reference: the reference's CPU algorithm (oracle) on this
     workload, bounded sample per step, all cores it can use (1: a single
@@ -823,6 +854,12 @@ def run_batch(args, wl):
                                                 "unit": "TFLOP/s", "peak": tf_peak, "ms": tms,
                                                 "kernel": "gemm_nt_kernel (mma.sync m16n8k16 BF16)"}
 
+    # ---- the single-instance engine's SpMV (the reference's CSR/CSC product
+    # pair in FP64) on the n = 200,000 portfolio, beside its two ceilings
+    spmv = None
+    if rank == 0 and not args.no_spmv:
+        spmv = single_instance_spmv(local)
+
     # ---- plain single-instance GPU ADMM on a few of the same instances
     plain_n = min(args.plain, B)
     plain_s, plain_iters = 0.0, []
@@ -906,6 +943,7 @@ def run_batch(args, wl):
             "solved": int(sum(d["solved"] for d in warm_inf)), "cold_start_fallbacks": fallbacks[0],
             "objective_error_vs_fp64_oracle": oracle_err,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "single_instance_spmv": spmv,
             "gpu_launches": int(launches), "clocks": clk.summary(),
         }
         line.update(info)
@@ -938,6 +976,8 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-spmv", action="store_true",
+                    help="skip the single-instance SpMV block of the batch workloads")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling case: set up the workload, run this many ADMM "
                          "iterations, print nothing else (for ncu)")

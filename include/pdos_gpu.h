@@ -28,6 +28,7 @@ enum {
 enum { PDOSGPU_FP64 = 0, PDOSGPU_FP32 = 1 };          /* storage/arithmetic */
 enum { PDOSGPU_SCALE_2NORM = 0, PDOSGPU_SCALE_RUIZ = 1 }; /* NORMALIZE=1 kind */
 enum { PDOSGPU_BATCH_SHARE = 0, PDOSGPU_BATCH_OWN = 1 };  /* batch layouts */
+enum { PDOSGPU_ENGINE_AUTO = 0, PDOSGPU_ENGINE_GRID = 1, PDOSGPU_ENGINE_CTA = 2 };
 
 typedef struct {
   int precision;   /* PDOSGPU_FP64 (default): every operation in double, the
@@ -45,14 +46,23 @@ typedef struct {
                         matrix layout, each keeping only its own values of
                         the entries that differ (same results, bit for bit);
                         PDOSGPU_BATCH_OWN gives every instance its own */
-  int reserved[4];
+  int engine;      /* pdos() / pdos_ex() only: PDOSGPU_ENGINE_AUTO (default)
+                      solves a small problem (m, n < 65,536, few nonzeros,
+                      VERBOSE=0, 2-norm scaling) in one launch of the batch
+                      kernel, one CTA running the whole ADMM loop, and any
+                      other on the grid engine; PDOSGPU_ENGINE_GRID and
+                      PDOSGPU_ENGINE_CTA force one of the two */
+  int reserved[3];
 } pdosgpu_options;
 
 typedef struct {
   int64_t admm_iters;   /* ADMM iterations run (pdos.c:94 loop index at exit) */
   int64_t cg_iters;     /* CG iterations summed over the solve */
   int solved;           /* 1 = "Solved", 0 = "Indeterminate" */
-  int pad;
+  int diverged;         /* 1: a residual or the gap became NaN/Inf (e.g. FP32
+                           storage overflowed); the solve stopped at that
+                           iteration instead of running to MAX_ITERS, and the
+                           status is "Indeterminate" */
   double p_res, d_res;  /* last DIMACS residuals (pdos.c:95-96), -1 if none */
   double p_obj, d_obj, eta;
   double lambda;        /* common.h:182 */
@@ -120,6 +130,12 @@ void *pdosgpu_stream(pdosgpu_work *w);
  * 4 / 5 = the SpMV kernel alone of the CG A / A' pass.  Leaves the iterate
  * undefined: call pdosgpu_reset() before solving again. */
 int pdosgpu_time_kernel(pdosgpu_work *w, int which, int reps, double *ms_per_launch);
+
+/* Roofline support: the device's FP64 fused multiply-add rate (FMA/s),
+ * measured with CUDA events on independent FMA chains over every SM.  The
+ * FP64 SpMV of accumByScaledA/ATrans (linAlg.h:70-115) executes one FMA per
+ * nonzero, so nnz / rate bounds its duration beside the HBM bound. */
+int pdosgpu_fp64_fma_rate(int device, double *fma_per_s);
 
 /* pdos() with explicit GPU options; info may be NULL. */
 Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt,
@@ -250,6 +266,15 @@ int pdosgpu_mlp_sync(pdosgpu_mlp *p);
  * a producer / MMA / epilogue warp split; 1 = tcgen05 with operands staged
  * by cp.async; 0 = mma.sync.  All three give the same products. */
 int pdosgpu_mlp_set_kernel(pdosgpu_mlp *p, int kind);
+/* Failure-path test of the bounded waits (cycles > 0; 0 turns it off): the
+ * next TMA-fed tensor-core products (kernel 2) first wait, for at most
+ * `cycles` clock cycles, on a barrier that nothing completes, before any
+ * copy or product is issued.  The wait runs out, each product records the
+ * timeout and frees its tensor memory without writing its output, and the
+ * following pdosgpu_mlp_sync returns PDOSGPU_ECUDA once (the flag is then
+ * cleared).  Every wait of the tensor-core kernels is bounded (about one
+ * second) in normal use; this exercises that path without a GPU fault. */
+int pdosgpu_mlp_test_wait_timeout(pdosgpu_mlp *p, int64_t cycles);
 void pdosgpu_mlp_free(pdosgpu_mlp *p);
 
 /* pdos() over `count` problems at once: sols[i] is what pdos(d[i], k[i])

@@ -25,16 +25,19 @@ PDOSGPU_SCALE_2NORM = 0
 PDOSGPU_SCALE_RUIZ = 1
 PDOSGPU_BATCH_SHARE = 0
 PDOSGPU_BATCH_OWN = 1
+PDOSGPU_ENGINE_AUTO = 0
+PDOSGPU_ENGINE_GRID = 1
+PDOSGPU_ENGINE_CTA = 2
 
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("scaling", c_int), ("device", c_int),
-                ("batch_layouts", c_int), ("reserved", c_int * 4)]
+                ("batch_layouts", c_int), ("engine", c_int), ("reserved", c_int * 3)]
 
 
 class Info(ctypes.Structure):
     _fields_ = [("admm_iters", c_int64), ("cg_iters", c_int64), ("solved", c_int),
-                ("pad", c_int), ("p_res", c_double), ("d_res", c_double),
+                ("diverged", c_int), ("p_res", c_double), ("d_res", c_double),
                 ("p_obj", c_double), ("d_obj", c_double), ("eta", c_double),
                 ("lambda_", c_double), ("setup_ms", c_double), ("solve_ms", c_double),
                 ("kernel_launches", c_int64)]
@@ -73,6 +76,7 @@ SIGNATURES = {
     "pdosgpu_free": (None, [c_void_p]),
     "pdosgpu_stream": (c_void_p, [c_void_p]),
     "pdosgpu_time_kernel": (c_int, [c_void_p, c_int, c_int, POINTER(c_double)]),
+    "pdosgpu_fp64_fma_rate": (c_int, [c_int, POINTER(c_double)]),
     "pdosgpu_csc_to_csr_f64": (c_int, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p, c_void_p, c_void_p]),
     "pdosgpu_spmv_f64": (c_int, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
@@ -116,6 +120,7 @@ SIGNATURES = {
     "pdosgpu_mlp_stream": (c_void_p, [c_void_p]),
     "pdosgpu_mlp_sync": (c_int, [c_void_p]),
     "pdosgpu_mlp_set_kernel": (c_int, [c_void_p, c_int]),
+    "pdosgpu_mlp_test_wait_timeout": (c_int, [c_void_p, c_int64]),
     "pdosgpu_mlp_free": (None, [c_void_p]),
     "pdos_batch": (c_int, [POINTER(POINTER(Data)), POINTER(POINTER(Cone)), c_int64,
                            POINTER(Options), POINTER(POINTER(Sol)), POINTER(Info)]),

@@ -3,9 +3,14 @@
 // once without (idxint = int, libpdosindir_i32.so).
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/pdos_gpu.h"
+
+namespace pdosgpu {
+int fail(int code, const std::string &msg);  // sets pdos_gpu_last_error()
+}
 
 namespace {
 
@@ -83,6 +88,42 @@ void set_status(Sol *sol, int solved) {
   std::strncpy(sol->status, solved ? "Solved" : "Indeterminate", sizeof(sol->status) - 1);
 }
 
+// Nonzeros up to which pdos() solves a problem with one CTA of the batch
+// kernel: every ADMM iteration then runs inside one launch with CTA
+// barriers only, where the grid engine launches 2k + 4 kernels per
+// iteration (k CG steps) and waits on each.
+constexpr int64_t kOneCtaMaxNnz = 65536;
+
+// pdos() through the one-CTA path: a batch of one instance, run to its stop
+// test in one launch of the persistent kernel at 1,024 threads.
+Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_options *opt, pdosgpu_info *info) {
+  pdosgpu_batch *b = NULL;
+  if (pdosgpu_batch_setup(&pr, 1, opt, 0, &b) != PDOSGPU_OK) return NULL;
+  const int blocks[5] = {1024, 1024, 1024, 1024, 1024};
+  Sol *sol = NULL;
+  pdosgpu_info inf;
+  if (pdosgpu_batch_set_blocks(b, blocks) == PDOSGPU_OK && pdosgpu_batch_solve(b) == PDOSGPU_OK) {
+    sol = new_sol(d->n, d->m);
+    if (sol && pdosgpu_batch_fetch(b, 0, 1, sol->x, sol->s, sol->y, &inf) != PDOSGPU_OK) {
+      freeSol(&sol);
+    } else if (sol) {
+      set_status(sol, inf.solved);
+      if (info) *info = inf;
+    }
+  }
+  pdosgpu_batch_free(b);
+  return sol;
+}
+
+bool use_one_cta(const pdosgpu_problem &pr, const pdosgpu_options *opt) {
+  const int engine = opt ? opt->engine : PDOSGPU_ENGINE_AUTO;
+  if (engine == PDOSGPU_ENGINE_GRID) return false;
+  const bool fits = pr.m <= 65535 && pr.n <= 65535 && !pr.verbose &&
+                    !(pr.normalize && opt && opt->scaling == PDOSGPU_SCALE_RUIZ);
+  if (engine == PDOSGPU_ENGINE_CTA) return fits;
+  return fits && pr.Ap[pr.n] <= kOneCtaMaxNnz;
+}
+
 }  // namespace
 
 extern "C" {
@@ -91,6 +132,11 @@ Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt, pdosgpu_i
   Wide w;
   pdosgpu_problem pr;
   if (!to_problem(d, k, w, pr)) return NULL;
+  if (opt && (opt->engine < PDOSGPU_ENGINE_AUTO || opt->engine > PDOSGPU_ENGINE_CTA)) {
+    pdosgpu::fail(PDOSGPU_EINVAL, "unknown engine");
+    return NULL;
+  }
+  if (use_one_cta(pr, opt)) return solve_one_cta(d, pr, opt, info);
   pdosgpu_work *work = NULL;
   if (pdosgpu_setup(&pr, opt, &work) != PDOSGPU_OK) return NULL;
   Sol *sol = NULL;

@@ -107,6 +107,14 @@ struct OpTop {
       s.cg_skip = 1;
       return;
     }
+    // A non-finite residual or gap (the iterate overflowed): the reference
+    // would run on to MAX_ITERS (pdos.c:94-107); stop here and say so.
+    if (!isfinite(s.p_res) || !isfinite(s.d_res) || !isfinite(s.eta)) {
+      s.diverged = 1;
+      s.done = 1;
+      s.cg_skip = 1;
+      return;
+    }
     s.qsold = tot[2];
     s.cg_iter = 0;
     s.cg_active = (s.cg_max > 0 && s.qsold > s.tol_sq) ? 1 : 0;

@@ -41,6 +41,24 @@ __global__ void gather_col_kernel_api(const int32_t *perm, const int32_t *col_of
 }
 }  // namespace setup
 
+// Eight independent FP64 fused multiply-add chains per thread: the device's
+// FP64 FMA issue rate, the second ceiling (beside HBM) of the FP64 SpMV,
+// which executes one FMA per nonzero.
+__global__ void fp64_fma_rate_kernel(double *sink, int iters) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1e-3 * (threadIdx.x + k);
+  const double mul = 0.999999999, add = 1e-12;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], mul, add);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += a[k];
+  if (t == -1.0) *sink = t;  // never true; keeps the chains live
+}
+
 static int check_device() {
   int count = 0;
   cudaError_t e = cudaGetDeviceCount(&count);
@@ -132,6 +150,39 @@ int pdosgpu_fetch(pdosgpu_work *w, double *x, double *s, double *y, pdosgpu_info
 void pdosgpu_free(pdosgpu_work *w) { delete w; }
 
 void *pdosgpu_stream(pdosgpu_work *w) { return (w && w->engine) ? w->engine->stream() : nullptr; }
+
+int pdosgpu_fp64_fma_rate(int device, double *fma_per_s) {
+  PDOS_TRY(check_device());
+  if (!fma_per_s) return fail(PDOSGPU_EINVAL, "NULL output");
+  PDOS_CUDA_TRY(cudaSetDevice(device));
+  int sms = 0;
+  PDOS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  cudaStream_t st = nullptr;
+  PDOS_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = PDOSGPU_OK;
+  const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+  double *sink = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
+      cudaMalloc(&sink, sizeof(double)) != cudaSuccess)
+    rc = fail(PDOSGPU_ECUDA, "event or buffer creation failed");
+  float ms = 0.f;
+  if (rc == PDOSGPU_OK) {
+    fp64_fma_rate_kernel<<<blocks, threads, 0, st>>>(sink, iters);  // warm-up
+    cudaEventRecord(e0, st);
+    fp64_fma_rate_kernel<<<blocks, threads, 0, st>>>(sink, iters);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.f)
+      rc = fail(PDOSGPU_ECUDA, "FMA rate kernel failed");
+  }
+  if (sink) cudaFree(sink);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  PDOS_TRY(rc);
+  *fma_per_s = (double)blocks * threads * 8.0 * iters / (ms / 1e3);
+  return PDOSGPU_OK;
+}
 
 int pdosgpu_time_kernel(pdosgpu_work *w, int which, int reps, double *ms_per_launch) {
   if (!w || !w->engine) return fail(PDOSGPU_EINVAL, "NULL workspace");

@@ -88,7 +88,7 @@ struct Inst {
 struct State {
   double pres_sq, by, p_res, d_res, p_obj, d_obj, eta;
   long long admm_iter, cg_total;
-  int solved, done, prepped, pad;
+  int solved, done, prepped, diverged;
 };
 
 template <typename T>
@@ -422,6 +422,14 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     if (S.p_res < I.eps * I.pscale && S.d_res < I.eps * I.dscale &&
         S.eta < I.eps * (1.0 + fabs(S.p_obj) + fabs(S.d_obj))) {
       S.solved = 1;
+      S.done = 1;
+      newly_done = true;
+      break;
+    }
+    // A non-finite residual or gap: this instance's iterate overflowed.  It
+    // stops here and frees its CTA; its neighbours never read its vectors.
+    if (!isfinite(S.p_res) || !isfinite(S.d_res) || !isfinite(S.eta)) {
+      S.diverged = 1;
       S.done = 1;
       newly_done = true;
       break;
@@ -1622,6 +1630,7 @@ int BatchEngine<T>::fetch(int64_t first, int64_t cnt, double *x, double *s, doub
       o.admm_iters = h[i].admm_iter;
       o.cg_iters = h[i].cg_total;
       o.solved = h[i].solved;
+      o.diverged = h[i].diverged;
       o.p_res = h[i].p_res;
       o.d_res = h[i].d_res;
       o.p_obj = h[i].p_obj;

@@ -123,6 +123,7 @@ struct DevState {
   long long admm_iter, cg_total;
   int cg_iter, cg_active, done, solved, evaluated;
   int cg_skip;  // done || !cg_active, read by the CG SpMV kernels
+  int diverged;  // a residual or the gap went non-finite: the solve stopped there
 };
 
 }  // namespace pdosgpu

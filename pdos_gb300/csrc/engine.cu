@@ -869,6 +869,7 @@ int Engine<T>::fetch(double *x, double *s, double *y, pdosgpu_info *info) {
     info->admm_iters = h.admm_iter;
     info->cg_iters = h.cg_total;
     info->solved = h.solved;
+    info->diverged = h.diverged;
     info->p_res = h.p_res;
     info->d_res = h.d_res;
     info->p_obj = h.p_obj;

@@ -191,11 +191,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
   return ok != 0;
 }
 
-// true if the phase completed within about a second of clock time
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity) {
+// true if the phase completed within `limit` clock cycles (default about a
+// second)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t addr, uint32_t parity, long long limit = kWaitCycles) {
   const long long t0 = clock64();
   while (!mbar_try_wait(addr, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 
@@ -430,11 +431,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
       : "memory");
 }
 
+// test_wait > 0 (failure-path test only): before any copy or product, the
+// CTA waits at most test_wait clock cycles on a barrier that nothing
+// completes; the wait runs out, the CTA records the timeout in *err, issues
+// nothing, frees its tensor memory and leaves its outputs unwritten.
 __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                const __grid_constant__ CUtensorMap tmB, int M,
-                                                               int N, int K, Epi ep, int *err) {
+                                                               int N, int K, Epi ep, int *err, long long test_wait) {
   extern __shared__ unsigned char raw[];
-  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint64_t full[kStages], empty[kStages], done, never;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail, s_issued;
   unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
@@ -452,6 +457,7 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(eb + 8 * i));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(db));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&never)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
@@ -466,6 +472,10 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
   const int nk = (K + TK - 1) / TK;
+  if (test_wait > 0) {  // a wait that nothing completes (failure-path test)
+    if (tid == 0 && !tc::mbar_wait_bounded((uint32_t)__cvta_generic_to_shared(&never), 0, test_wait)) s_fail = 1;
+    __syncthreads();
+  }
 
   if (warp == 0) {  // producer: lane 0 streams the stages
     if (lane == 0) {
@@ -489,7 +499,7 @@ __global__ void __launch_bounds__(kThreads) gemm_nt_tma_kernel(const __grid_cons
     __syncwarp();
   } else if (warp == 1) {  // products: lane 0 issues
     if (lane == 0) {
-    for (int kt = 0; kt < nk; ++kt) {
+    for (int kt = 0; kt < nk && !*(volatile int *)&s_fail; ++kt) {
       const int st = kt % kStages;
       if (!tc::mbar_wait_bounded(fb + 8 * st, (uint32_t)((kt / kStages) & 1))) {
         s_fail = 1;
@@ -700,6 +710,7 @@ class Net {
   int time_forward(int B, int reps, double *ms, double *flops);
   int set_gemm(int kind);
   int check();
+  long long test_wait_ = 0;  // failure-path test of the bounded waits (0: off)
   int encode_map(CUtensorMap *map, const bf16 *p, int ld, int rows, int K, int box_rows);
   cudaStream_t stream_ = nullptr;
   int64_t launches = 0;
@@ -733,7 +744,8 @@ int Net::gemm(const bf16 *A, int lda, const bf16 *B, int ldb, int M, int N, int 
     PDOS_TRY(encode_map(&ma, A, lda, M, K, tma::TM));
     PDOS_TRY(encode_map(&mb, B, ldb, N, K, tma::TN));
     dim3 grid((N + tma::TN - 1) / tma::TN, (M + tma::TM - 1) / tma::TM);
-    tma::gemm_nt_tma_kernel<<<grid, tma::kThreads, tma::kSmemBytes, stream_>>>(ma, mb, M, N, K, ep, tc_err_);
+    tma::gemm_nt_tma_kernel<<<grid, tma::kThreads, tma::kSmemBytes, stream_>>>(ma, mb, M, N, K, ep, tc_err_,
+                                                                              test_wait_);
   } else if (gemm_kind_ == 1) {
     dim3 grid((N + tc::TN - 1) / tc::TN, (M + tc::TM - 1) / tc::TM);
     tc::gemm_nt_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, stream_>>>(A, lda, B, ldb, M, N, K, ep, tc_err_);
@@ -796,7 +808,11 @@ int Net::check() {
   int h = 0;
   PDOS_CUDA_TRY(cudaMemcpyAsync(&h, tc_err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
   PDOS_CUDA_TRY(cudaStreamSynchronize(stream_));
-  if (h) return fail(PDOSGPU_ECUDA, "a tensor-core product timed out waiting for its operands");
+  if (h) {  // reported once: the flag is cleared for the next products
+    PDOS_CUDA_TRY(cudaMemsetAsync(tc_err_, 0, sizeof(int), stream_));
+    PDOS_CUDA_TRY(cudaStreamSynchronize(stream_));
+    return fail(PDOSGPU_ECUDA, "a tensor-core product timed out waiting for its operands");
+  }
   return PDOSGPU_OK;
 }
 
@@ -1070,6 +1086,14 @@ int pdosgpu_mlp_sync(pdosgpu_mlp *p) {
 int pdosgpu_mlp_set_kernel(pdosgpu_mlp *p, int kind) {
   if (!p) return fail(PDOSGPU_EINVAL, "NULL network");
   return p->net.set_gemm(kind);
+}
+
+int pdosgpu_mlp_test_wait_timeout(pdosgpu_mlp *p, int64_t cycles) {
+  if (!p) return fail(PDOSGPU_EINVAL, "NULL network");
+  if (cycles < 0) return fail(PDOSGPU_EINVAL, "cycles must be nonnegative");
+  PDOS_TRY(p->net.check());
+  p->net.test_wait_ = cycles;
+  return PDOSGPU_OK;
 }
 
 void pdosgpu_mlp_free(pdosgpu_mlp *p) { delete p; }

@@ -21,7 +21,10 @@ _PRECISION = {"fp64": _lib.PDOSGPU_FP64, "fp32": _lib.PDOSGPU_FP32}
 _SCALING = {"2norm": _lib.PDOSGPU_SCALE_2NORM, "ruiz": _lib.PDOSGPU_SCALE_RUIZ}
 
 
-def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True):
+_ENGINE = {"auto": _lib.PDOSGPU_ENGINE_AUTO, "grid": _lib.PDOSGPU_ENGINE_GRID, "cta": _lib.PDOSGPU_ENGINE_CTA}
+
+
+def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True, engine="auto"):
     if precision not in _PRECISION:
         raise ValueError(f"precision must be one of {sorted(_PRECISION)}")
     if scaling not in _SCALING:
@@ -32,6 +35,9 @@ def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True
     opt.scaling = _SCALING[scaling]
     opt.device = device
     opt.batch_layouts = _lib.PDOSGPU_BATCH_SHARE if share_layouts else _lib.PDOSGPU_BATCH_OWN
+    if engine not in _ENGINE:
+        raise ValueError(f"engine must be one of {sorted(_ENGINE)}")
+    opt.engine = _ENGINE[engine]
     return opt
 
 
@@ -372,22 +378,31 @@ def pdos_batch_call(probs, precision=None, libname="libpdosindir.so"):
     return out
 
 
+def fp64_fma_rate(device=0):
+    """The device's FP64 fused multiply-add rate, FMA/s (pdosgpu_fp64_fma_rate)."""
+    lib = _lib.load()
+    r = ctypes.c_double()
+    _lib.check(lib.pdosgpu_fp64_fma_rate(int(device), ctypes.byref(r)), "pdosgpu_fp64_fma_rate", lib)
+    return r.value
+
+
 def solve_problem(prob, precision="fp64", scaling="2norm"):
     """Set up, solve, fetch and free."""
     with Workspace(prob, precision, scaling) as ws:
         return ws.solve().fetch()
 
 
-def pdos_call(prob, precision=None, scaling=None, libname="libpdosindir.so", device=None):
+def pdos_call(prob, precision=None, scaling=None, libname="libpdosindir.so", device=None, engine=None):
     """Solve through the reference-compatible ``pdos()`` / ``pdos_ex()``
-    (``pdos_ex`` when a precision, scaling or device is given)."""
+    (``pdos_ex`` when a precision, scaling, device or engine is given;
+    engine: "auto", "grid" or "cta")."""
     lib = _lib.load(libname)
     mar = Marshalled(prob)
-    if precision is None and scaling is None and device is None:
+    if precision is None and scaling is None and device is None and engine is None:
         solp = lib.pdos(ctypes.byref(mar.data), ctypes.byref(mar.cone))
         info = None
     else:
-        opt = make_options(precision or "fp64", scaling or "2norm", device or 0)
+        opt = make_options(precision or "fp64", scaling or "2norm", device or 0, engine=engine or "auto")
         info = _lib.Info()
         solp = lib.pdos_ex(ctypes.byref(mar.data), ctypes.byref(mar.cone), ctypes.byref(opt),
                            ctypes.byref(info))
@@ -399,6 +414,7 @@ def pdos_call(prob, precision=None, scaling=None, libname="libpdosindir.so", dev
     if info is not None:
         out["iters"] = info.admm_iters
         out["cg_iters"] = info.cg_iters
+        out["info"] = info.as_dict()
     return out
 
 

@@ -93,6 +93,12 @@ class Net:
     def sync(self):
         _lib.check(self.lib.pdosgpu_mlp_sync(self._p), "pdosgpu_mlp_sync", self.lib)
 
+    def test_wait_timeout(self, cycles):
+        """Failure-path test of the kernels' bounded waits (0 turns it off)."""
+        _lib.check(self.lib.pdosgpu_mlp_test_wait_timeout(self._p, int(cycles)), "pdosgpu_mlp_test_wait_timeout",
+                   self.lib)
+        return self
+
     def close(self):
         if self._p:
             self.lib.pdosgpu_mlp_free(self._p)

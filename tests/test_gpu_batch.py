@@ -329,3 +329,32 @@ def test_family_groups_share_a_layout_with_identical_bits(built_lib, torch_cuda,
     assert [d["admm_iters"] for d in inf1] == [d["admm_iters"] for d in inf2]
     assert np.array_equal(again[0], x2)
     assert all(d["solved"] for d in inf2)
+
+
+def test_overflowing_instance_is_flagged_diverged_without_touching_neighbours(built_lib, torch_cuda):
+    """An instance whose data is finite in double but overflows FP32 storage
+    (an entry of 1e39) comes back from the FP32 batch flagged diverged at
+    its first stop test, instead of holding its CTA for MAX_ITERS; its
+    neighbours' results are the bits they get without it.  The
+    single-instance FP32 engine flags it the same way."""
+    import dataclasses
+    from pdos_gb300 import generators as g
+    from pdos_gb300.solver import Batch, Workspace
+    P = dict(EPS_ABS=1e-4, VERBOSE=0, MAX_ITERS=3000)
+    good = [g.portfolio(200, 20, 0.2, seed=s, params=P) for s in (61, 62)]
+    bad = g.portfolio(200, 20, 0.2, seed=63, params=P)
+    ax = bad.Ax.copy()
+    ax[5] = 1e39
+    bad = dataclasses.replace(bad, Ax=ax)
+    with Batch([good[0], bad, good[1]], precision="fp32") as b:
+        x, s, y, inf = b.solve().fetch_all()
+    with Batch(good, precision="fp32") as ref:
+        xr, sr, yr, infr = ref.solve().fetch_all()
+    assert inf[1]["diverged"] == 1 and inf[1]["solved"] == 0 and inf[1]["admm_iters"] <= 1
+    assert inf[0]["diverged"] == inf[2]["diverged"] == 0 and inf[0]["solved"] == inf[2]["solved"] == 1
+    n0, nb, m0, mb = good[0].n, bad.n, good[0].m, bad.m
+    assert np.array_equal(x[:n0], xr[:n0]) and np.array_equal(x[n0 + nb:], xr[n0:])
+    assert np.array_equal(y[:m0], yr[:m0]) and np.array_equal(y[m0 + mb:], yr[m0:])
+    with Workspace(bad, "fp32") as w:
+        r = w.solve().fetch()
+    assert r["info"]["diverged"] == 1 and r["status"] == "Indeterminate" and r["iters"] <= 1

@@ -134,3 +134,27 @@ def test_learned_warm_start_beats_cold_start(built_lib, torch_cuda, port):
         oh = float(p.c @ hi["x"])
         for r in (a, b):
             assert abs(float(p.c @ r["x"]) - oh) <= 1e-3 * max(1.0, abs(oh))
+
+
+def test_bounded_wait_reports_timeout_and_gpu_stays_usable(built_lib, torch_cuda):
+    """The tensor-core kernels bound every mbarrier wait.  With the test knob
+    set, each CTA of the TMA-fed kernel first waits on a barrier that nothing
+    completes, gives up after 20,000 cycles, frees its tensor memory and
+    reports; pdosgpu_mlp_sync returns the error once, and the next forward
+    pass on the same GPU gives the bits of the pass before the failure."""
+    torch = torch_cuda
+    dims, B = (200, 256, 256, 300), 64
+    net, _, _, x, _ = _setup(torch, dims, B, seed=5)
+    net.set_kernel(2)
+    xd = torch.from_numpy(x).cuda()
+    y0 = torch.empty((B, dims[3]), dtype=torch.float32, device="cuda")
+    net.forward(xd, y0)
+    net.test_wait_timeout(20000)
+    y1 = torch.full((B, dims[3]), 7.0, dtype=torch.float32, device="cuda")
+    with pytest.raises(RuntimeError, match="timed out"):
+        net.forward(xd, y1)
+    net.test_wait_timeout(0)
+    y2 = torch.empty((B, dims[3]), dtype=torch.float32, device="cuda")
+    net.forward(xd, y2)
+    assert torch.equal(y0, y2)
+    net.close()
