@@ -43,3 +43,38 @@ def gather_results(results, indices, count, dist):
     if any(r is None for r in out):
         raise RuntimeError("an instance was solved by no rank")
     return out
+
+
+def all_gather_rows(local, indices, count, dist, device="cpu"):
+    """Every rank gets every rank's rows in instance order: a (count, width)
+    float64 array assembled from each rank's `local` rows (row j belongs to
+    instance indices[j]).  One padded all_gather of a tensor per array and
+    one of the indices -- gloo for CPU tensors, nccl for CUDA tensors.  Used
+    to share the training data that the ranks solved in parts."""
+    import numpy as np
+    import torch
+    world = dist.get_world_size()
+    local = np.asarray(local, np.float64)
+    width = local.shape[1]
+    n_local = len(indices)
+    sizes = [torch.zeros(1, dtype=torch.int64, device=device) for _ in range(world)]
+    dist.all_gather(sizes, torch.tensor([n_local], dtype=torch.int64, device=device))
+    cap = max(int(s.item()) for s in sizes)
+    idx = torch.full((cap,), -1, dtype=torch.int64, device=device)
+    idx[:n_local] = torch.as_tensor(np.asarray(indices, np.int64), device=device)
+    rows = torch.zeros((cap, width), dtype=torch.float64, device=device)
+    rows[:n_local] = torch.as_tensor(local, device=device)
+    all_idx = [torch.empty_like(idx) for _ in range(world)]
+    all_rows = [torch.empty_like(rows) for _ in range(world)]
+    dist.all_gather(all_idx, idx)
+    dist.all_gather(all_rows, rows)
+    out = np.full((count, width), np.nan)
+    seen = np.zeros(count, bool)
+    for ix, rw, sz in zip(all_idx, all_rows, sizes):
+        k = int(sz.item())
+        ii = ix[:k].cpu().numpy()
+        out[ii] = rw[:k].cpu().numpy()
+        seen[ii] = True
+    if not seen.all():
+        raise RuntimeError("an instance's rows came from no rank")
+    return out

@@ -7,7 +7,7 @@ import socket
 import numpy as np
 import pytest
 
-from pdos_gb300.shard import gather_results, shard_instances
+from pdos_gb300.shard import all_gather_rows, gather_results, shard_instances
 
 
 def test_partition_is_disjoint_complete_and_balanced():
@@ -60,3 +60,38 @@ def test_two_gloo_ranks_gather_every_result_in_order():
     assert owners == {0, 1}
     for r in out:
         assert r["instance"] in shard_instances(costs, 2, r["rank"])
+
+
+def _training_rows(i, width):
+    """Stand-in for instance i's solution (x, y, s) rows."""
+    return np.sin(np.arange(width) * 0.37 + i) * (1.0 + i)
+
+
+def _rank_rows(rank, world, port, count, width, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    mine = shard_instances([1] * count, world, rank)
+    local = np.stack([_training_rows(i, width) for i in mine])
+    full = all_gather_rows(local, mine, count, dist)
+    q.put((rank, full))
+    dist.destroy_process_group()
+
+
+def test_sharded_training_data_equals_unsharded():
+    """The training set solved in parts by two ranks and gathered with
+    all_gather_rows is, on every rank, the array one rank would make alone."""
+    import torch.multiprocessing as mp
+    count, width = 45, 13
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_rows, args=(r, 2, port, count, width, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in range(2))
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    want = np.stack([_training_rows(i, width) for i in range(count)])
+    assert np.array_equal(got[0], want) and np.array_equal(got[1], want)
