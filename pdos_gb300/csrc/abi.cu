@@ -95,14 +95,13 @@ void set_status(Sol *sol, int solved) {
 constexpr int64_t kOneCtaMaxNnz = 65536;
 
 // pdos() through the one-CTA path: a batch of one instance, run to its stop
-// test in one launch of the persistent kernel at 1,024 threads.
+// test in one launch of the persistent kernel (CTA size by size class).
 Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_options *opt, pdosgpu_info *info) {
   pdosgpu_batch *b = NULL;
   if (pdosgpu_batch_setup(&pr, 1, opt, 0, &b) != PDOSGPU_OK) return NULL;
-  const int blocks[5] = {1024, 1024, 1024, 1024, 1024};
   Sol *sol = NULL;
   pdosgpu_info inf;
-  if (pdosgpu_batch_set_blocks(b, blocks) == PDOSGPU_OK && pdosgpu_batch_solve(b) == PDOSGPU_OK) {
+  if (pdosgpu_batch_solve(b) == PDOSGPU_OK) {
     sol = new_sol(d->n, d->m);
     if (sol && pdosgpu_batch_fetch(b, 0, 1, sol->x, sol->s, sol->y, &inf) != PDOSGPU_OK) {
       freeSol(&sol);

@@ -106,14 +106,17 @@ struct Dev {
 };
 
 // Staging regions of one class, in elements of T: in dynamic shared memory,
-// or (global != 0) in the CTA's region of Dev::gscratch.
+// or (global != 0) in the CTA's region of Dev::gscratch.  A global-staging
+// class also keeps, in dynamic shared memory, room for the one vector a
+// product gathers from (gs elements): instances whose max(m, n) fits it
+// gather from shared memory, larger ones from their global region.
 struct Smem {
-  int32_t g1, g2, tt, pb, global;
+  int32_t g1, g2, tt, pb, global, gs;
   __host__ __device__ size_t stride() const {  // elements per CTA region, 128-byte multiples
     return ((size_t)g1 + g2 + tt + pb + 31) & ~(size_t)31;
   }
   size_t need(size_t elem) const { return elem * ((size_t)g1 + g2 + tt + pb); }
-  size_t bytes(size_t elem) const { return global ? 0 : need(elem); }
+  size_t bytes(size_t elem) const { return global ? elem * (size_t)gs : need(elem); }
 };
 
 // Base of a CTA's staging regions.  A compile-time choice, so that kernels
@@ -132,8 +135,13 @@ __device__ __forceinline__ T warp_sum_t(T v) {
   return v;
 }
 
-// Block sums of N values; every thread adds the warp partials in the same
-// fixed order, so all threads get identical totals.  The barrier after the
+// Block sums of N values.  Each warp sums its lanes with a xor butterfly,
+// lane 0 stores the warp's partial, and after the barrier every warp loads
+// the W partials into its lanes and runs the same butterfly: a fixed order,
+// and since floating-point addition commutes every lane of every warp ends
+// with the same bits.  (Summing the W partials one by one in every thread
+// would cost W times as many FP64 additions, which the GB300's narrow FP64
+// pipe turns into microseconds per reduction.)  The barrier after the
 // partials are written also orders every earlier shared-memory write.
 // Callers alternate between two scratch halves (Reduce below): the next use
 // of a half comes after another reduction's barrier, so no second barrier
@@ -150,12 +158,7 @@ __device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < N; ++k) {
-    double t = 0.0;
-#pragma unroll 8
-    for (int w = 0; w < W; ++w) t += scratch[k * W + w];
-    v[k] = t;
-  }
+  for (int k = 0; k < N; ++k) v[k] = warp_sum(lane < W ? scratch[k * W + lane] : 0.0);
 }
 
 // Two scratch halves of 3 * BLOCK/32 doubles, used in turn.
@@ -341,9 +344,15 @@ __device__ __forceinline__ T soc_rule(T v, bool is_head, T head, T tail) {
   return is_head ? half : half * v / tail;
 }
 
-template <typename T, int BLOCK>
+// SG (global staging only): the vector each product gathers from is first
+// copied into shared memory (gs), so the gathers hit shared memory while the
+// staging regions stay in global memory.  The top pass then runs as two
+// products (y, then u) instead of one with two source vectors: each row's
+// two sums are the same chains of fused multiply-adds as in the one-pass
+// form, so the results are bit-identical.
+template <typename T, int BLOCK, bool SG = false>
 __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int iter_cap, T *g1,
-                               T *g2, T *tt, T *pbuf, double *scratch) {
+                               T *g2, T *tt, T *pbuf, double *scratch, T *gs = nullptr) {
   const int tid = threadIdx.x;
   const int m = I.m, n = I.n, f = I.f, l = I.l;
   T *__restrict__ x = B.x + I.col0;
@@ -378,10 +387,13 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
   };
 
   if (!S.prepped) {  // A x0: residual, u and b'y of iteration 0
-    for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
+    for (int j = tid; j < n; j += BLOCK) {
+      if (SG) gs[j] = x[j];
+      else g1[j] = x[j];
+    }
     __syncthreads();
     double red[2] = {0.0, 0.0};
-    hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int r, T a, T) {
+    hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, SG ? gs : g1, SG ? gs : g1, pbuf, [&](int r, T a, T) {
       ax[r] = a;
       const T sv = s[r], bv = b[r], yv = y[r];
       const T pr = ((sv - bv) + a) / D[r];
@@ -398,13 +410,8 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
   bool newly_done = false;
   for (int it = 0; it < iter_cap; ++it) {
     // ---- top: A' on (y, u): dual residual, c'x, CG start; stop test
-    for (int r = tid; r < m; r += BLOCK) {
-      g1[r] = y[r];
-      g2[r] = u[r];
-    }
-    __syncthreads();
     double top[3] = {0.0, 0.0, 0.0};
-    hyb_product<T, BLOCK, 2>(I.hT, I.At, I.pvT, g1, g2, pbuf, [&](int j, T sy, T su) {
+    auto top_row = [&](int j, T sy, T su) {
       const T cj = c[j];
       const T dr = (cj + sy) / E[j];
       top[0] += (double)dr * (double)dr;
@@ -412,7 +419,23 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       const T qj = (-lam) * cj + (-su);
       q[j] = qj;
       top[2] += (double)qj * (double)qj;
-    });
+    };
+    if (SG) {  // A'y into tt, then A'u with the epilogue
+      for (int r = tid; r < m; r += BLOCK) gs[r] = y[r];
+      __syncthreads();
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, gs, gs, pbuf, [&](int j, T sy, T) { tt[j] = sy; });
+      __syncthreads();
+      for (int r = tid; r < m; r += BLOCK) gs[r] = u[r];
+      __syncthreads();
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, gs, gs, pbuf, [&](int j, T su, T) { top_row(j, tt[j], su); });
+    } else {
+      for (int r = tid; r < m; r += BLOCK) {
+        g1[r] = y[r];
+        g2[r] = u[r];
+      }
+      __syncthreads();
+      hyb_product<T, BLOCK, 2>(I.hT, I.At, I.pvT, g1, g2, pbuf, top_row);
+    }
     reduce(top);
     S.p_res = sqrt(S.pres_sq);
     S.d_res = sqrt(top[0]);
@@ -439,14 +462,23 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
     int cg_iter = 0;
     bool active = I.cg_max > 0 && qsold > I.tol_sq;
     if (active) {
-      for (int j = tid; j < n; j += BLOCK) g1[j] = q[j];  // p = q
+      for (int j = tid; j < n; j += BLOCK) {  // p = q
+        const T qj = q[j];
+        g1[j] = qj;
+        if (SG) gs[j] = qj;
+      }
       __syncthreads();
     }
     while (active) {
-      hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int r, T a, T) { g2[r] = a; });
+      hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, SG ? gs : g1, SG ? gs : g1, pbuf,
+                               [&](int r, T a, T) { g2[r] = a; });
       __syncthreads();
+      if (SG) {  // A p is the next gather source
+        for (int r = tid; r < m; r += BLOCK) gs[r] = g2[r];
+        __syncthreads();
+      }
       double pt[1] = {0.0};
-      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, g2, g2, pbuf, [&](int j, T a, T) {
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, SG ? gs : g2, SG ? gs : g2, pbuf, [&](int j, T a, T) {
         const T pj = g1[j];
         const T tj = pj + a;
         tt[j] = tj;
@@ -477,15 +509,22 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
       if (active) {
         const T beta = (T)ratio;
 #pragma unroll 4
-        for (int j = tid; j < n; j += BLOCK) g1[j] = beta * g1[j] + q[j];
+        for (int j = tid; j < n; j += BLOCK) {
+          const T pj = beta * g1[j] + q[j];
+          g1[j] = pj;
+          if (SG) gs[j] = pj;
+        }
         __syncthreads();
       }
     }
     // ---- A x: s~ = b - Ax, relax, s = s~ - lam y; zero / orthant rows done
-    for (int j = tid; j < n; j += BLOCK) g1[j] = x[j];
+    for (int j = tid; j < n; j += BLOCK) {
+      if (SG) gs[j] = x[j];
+      else g1[j] = x[j];
+    }
     __syncthreads();
     double fin[2] = {0.0, 0.0};
-    hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int r, T a, T) {
+    hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, SG ? gs : g1, SG ? gs : g1, pbuf, [&](int r, T a, T) {
       T stv = b[r] + (-a);
       stv = alpha * stv + oma * s[r];
       T v = stv - lam * y[r];
@@ -555,12 +594,21 @@ __device__ void solve_instance(const Dev<T> &B, const Inst &I, State *gst, int i
   }
 }
 
-template <typename T, int BLOCK, bool GLOBAL>
+// Staging modes of a kernel instantiation: 0 = everything in shared memory;
+// 1 = regions in global memory, the gather vector in shared memory (a
+// global-staging class whose every member's max(m, n) fits); 2 = regions and
+// gathers in global memory.  One mode per kernel keeps one code path, and
+// its registers, per instantiation.
+constexpr int kStageShared = 0, kStageGlobalSG = 1, kStageGlobal = 2;
+
+template <typename T, int BLOCK, int MODE>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
+  constexpr bool GLOBAL = MODE != kStageShared;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double scratch[2 * 3 * (BLOCK / 32)];
   __shared__ Inst s_inst;
   __shared__ int s_k;
+  T *gs = reinterpret_cast<T *>(smem_raw);  // global class: the gather vector
   T *g1 = staging_base<T, GLOBAL>(sm, smem_raw, B.gscratch);
   T *g2 = g1 + sm.g1;
   T *tt = g2 + sm.g2;
@@ -577,19 +625,22 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_admm_kernel(Dev<T> 
       reinterpret_cast<int32_t *>(&s_inst)[threadIdx.x] =
           reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
     __syncthreads();
-    solve_instance<T, BLOCK>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch);
+    solve_instance<T, BLOCK, MODE == kStageGlobalSG>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch,
+                                                     gs);
   }
 }
 
 // The two CG products alone (u = A p, t = p + A'u), `reps` times for every
 // instance of a class, for the roofline of the batch's SpMV: no reductions,
 // no stop test, the iterate untouched (p is the current x).
-template <typename T, int BLOCK, bool GLOBAL>
+template <typename T, int BLOCK, int MODE>
 __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev<T> B, int cls, Smem sm,
                                                                               int reps) {
+  constexpr bool GLOBAL = MODE != kStageShared;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Inst s_inst;
   __shared__ int s_k;
+  T *gs = reinterpret_cast<T *>(smem_raw);  // global class: the gather vector
   T *g1 = staging_base<T, GLOBAL>(sm, smem_raw, B.gscratch);
   T *g2 = g1 + sm.g1;
   T *tt = g2 + sm.g2;
@@ -608,12 +659,23 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev
     __syncthreads();
     const Inst &I = s_inst;
     const T *x = B.x + I.col0;
+    constexpr bool sg = MODE == kStageGlobalSG;  // gathers from shared memory
     for (int j = threadIdx.x; j < I.n; j += BLOCK) g1[j] = x[j];
     __syncthreads();
     for (int r = 0; r < reps; ++r) {
-      hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, g1, g1, pbuf, [&](int row, T a, T) { g2[row] = a; });
+      if (sg) {
+        for (int j = threadIdx.x; j < I.n; j += BLOCK) gs[j] = g1[j];
+        __syncthreads();
+      }
+      hyb_product<T, BLOCK, 1>(I.hA, I.A, I.pvA, sg ? gs : g1, sg ? gs : g1, pbuf,
+                               [&](int row, T a, T) { g2[row] = a; });
       __syncthreads();
-      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, g2, g2, pbuf, [&](int j, T a, T) { tt[j] = g1[j] + a; });
+      if (sg) {
+        for (int j = threadIdx.x; j < I.m; j += BLOCK) gs[j] = g2[j];
+        __syncthreads();
+      }
+      hyb_product<T, BLOCK, 1>(I.hT, I.At, I.pvT, sg ? gs : g2, sg ? gs : g2, pbuf,
+                               [&](int j, T a, T) { tt[j] = g1[j] + a; });
       __syncthreads();
     }
   }
@@ -736,26 +798,45 @@ inline double now_ms() {
 template <typename T>
 using KernelOf = void (*)(Dev<T>, int, Smem, int);
 
-// The persistent ADMM kernel and the product timing kernel of one CTA size,
-// staging in shared or in global memory (nullptr: unsupported size).
-template <typename T>
-KernelOf<T> admm_kernel_for(int block, bool global) {
+// The persistent ADMM kernel and the product timing kernel of one CTA size
+// and staging mode (nullptr: unsupported size).
+template <typename T, int MODE>
+KernelOf<T> admm_kernel_mode(int block) {
   switch (block) {
-    case 128: return global ? batch_admm_kernel<T, 128, true> : batch_admm_kernel<T, 128, false>;
-    case 256: return global ? batch_admm_kernel<T, 256, true> : batch_admm_kernel<T, 256, false>;
-    case 512: return global ? batch_admm_kernel<T, 512, true> : batch_admm_kernel<T, 512, false>;
-    case 1024: return global ? batch_admm_kernel<T, 1024, true> : batch_admm_kernel<T, 1024, false>;
+    case 128: return batch_admm_kernel<T, 128, MODE>;
+    case 256: return batch_admm_kernel<T, 256, MODE>;
+    case 512: return batch_admm_kernel<T, 512, MODE>;
+    case 1024: return batch_admm_kernel<T, 1024, MODE>;
     default: return nullptr;
   }
 }
-template <typename T>
-KernelOf<T> products_kernel_for(int block, bool global) {
+template <typename T, int MODE>
+KernelOf<T> products_kernel_mode(int block) {
   switch (block) {
-    case 128: return global ? batch_products_kernel<T, 128, true> : batch_products_kernel<T, 128, false>;
-    case 256: return global ? batch_products_kernel<T, 256, true> : batch_products_kernel<T, 256, false>;
-    case 512: return global ? batch_products_kernel<T, 512, true> : batch_products_kernel<T, 512, false>;
-    case 1024: return global ? batch_products_kernel<T, 1024, true> : batch_products_kernel<T, 1024, false>;
+    case 128: return batch_products_kernel<T, 128, MODE>;
+    case 256: return batch_products_kernel<T, 256, MODE>;
+    case 512: return batch_products_kernel<T, 512, MODE>;
+    case 1024: return batch_products_kernel<T, 1024, MODE>;
     default: return nullptr;
+  }
+}
+inline int stage_mode(const Smem &sm) {
+  return !sm.global ? kStageShared : (sm.gs > 0 ? kStageGlobalSG : kStageGlobal);
+}
+template <typename T>
+KernelOf<T> admm_kernel_for(int block, const Smem &sm) {
+  switch (stage_mode(sm)) {
+    case kStageShared: return admm_kernel_mode<T, kStageShared>(block);
+    case kStageGlobalSG: return admm_kernel_mode<T, kStageGlobalSG>(block);
+    default: return admm_kernel_mode<T, kStageGlobal>(block);
+  }
+}
+template <typename T>
+KernelOf<T> products_kernel_for(int block, const Smem &sm) {
+  switch (stage_mode(sm)) {
+    case kStageShared: return products_kernel_mode<T, kStageShared>(block);
+    case kStageGlobalSG: return products_kernel_mode<T, kStageGlobalSG>(block);
+    default: return products_kernel_mode<T, kStageGlobal>(block);
   }
 }
 
@@ -1306,7 +1387,7 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
   auto r4 = [](int32_t v) { return (v + 3) & ~3; };
   for (int64_t i = 0; i < cnt; ++i) {
     Inst &I = inst_h_[first + i];
-    const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0};
+    const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0, 0};
     if (own.need(sizeof(T)) > (size_t)kSmemLimit) I.cls = kGlobalClass;
   }
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // the wave's set-up arrays are released next
@@ -1378,15 +1459,18 @@ int BatchEngine<T>::commit() {
   for (int k = 0; k < kClasses; ++k) {
     auto &mv = members[k];
     std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) { return nnz_h_[a] > nnz_h_[bb]; });
-    Smem sm{0, 0, 0, 0, k == kGlobalClass ? 1 : 0};
+    Smem sm{0, 0, 0, 0, k == kGlobalClass ? 1 : 0, 0};
+    const int32_t gs_cap = (int32_t)(kSmemLimit / sizeof(T)) & ~3;  // gather vector in shared memory
     for (int32_t i : mv) {
       const Inst &I = inst_h_[i];
       sm.g1 = std::max(sm.g1, std::max(I.m, I.n));
       sm.g2 = std::max(sm.g2, I.m);
       sm.tt = std::max(sm.tt, I.n);
       sm.pb = std::max(sm.pb, 2 * std::max(I.A.npieces, I.At.npieces));
+      if (sm.global) sm.gs = std::max(sm.gs, r4(std::max(I.m, I.n)));
     }
-    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb), sm.global};
+    if (sm.gs > gs_cap) sm.gs = 0;  // some member's vectors do not fit: gathers from global memory
+    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb), sm.global, sm.gs};
     smem_[k] = sm;
     block_[k] = k == 0 ? 128 : (k == 1 ? 256 : 512);
     order.insert(order.end(), mv.begin(), mv.end());
@@ -1476,7 +1560,7 @@ int BatchEngine<T>::configure(int cls, int block) {
     if (smem_[cls].global) grid_[cls] = std::min(grid_[cls], gregions_);
     return PDOSGPU_OK;
   };
-  auto kernel = admm_kernel_for<T>(block, smem_[cls].global != 0);
+  auto kernel = admm_kernel_for<T>(block, smem_[cls]);
   if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
   return go(kernel);
 }
@@ -1485,7 +1569,7 @@ template <typename T>
 int BatchEngine<T>::launch_class(int cls, int block, int iter_cap, cudaStream_t st) {
   const Smem sm = smem_[cls];
   const size_t bytes = sm.bytes(sizeof(T));
-  auto kernel = admm_kernel_for<T>(block, sm.global != 0);
+  auto kernel = admm_kernel_for<T>(block, sm);
   if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
   kernel<<<grid_[cls], block, bytes, st>>>(dev_, cls, sm, iter_cap);
   PDOS_CUDA_TRY(cudaGetLastError());
@@ -1745,7 +1829,7 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
     PDOS_CUDA_TRY(cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st));
     for (int k = 0; k < kClasses; ++k) {
       if (class_begin_h_[k + 1] == class_begin_h_[k]) continue;
-      auto kernel = products_kernel_for<T>(block_[k], smem_[k].global != 0);
+      auto kernel = products_kernel_for<T>(block_[k], smem_[k]);
       if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
       PDOS_TRY(go(k, block_[k], kernel));
     }
