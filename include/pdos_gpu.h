@@ -52,7 +52,13 @@ typedef struct {
                       kernel, one CTA running the whole ADMM loop, and any
                       other on the grid engine; PDOSGPU_ENGINE_GRID and
                       PDOSGPU_ENGINE_CTA force one of the two */
-  int reserved[3];
+  int batch_long_row; /* batches only: rows with more nonzeros than this are
+                         cut into warp-wide pieces, shorter ones share
+                         32-row slices (0: 128; else a multiple of 4 in
+                         [4, 1024]) */
+  int batch_piece;    /* batches only: nonzeros per piece at most (0: 1,024;
+                         else a multiple of 4 in [64, 16384]) */
+  int reserved[1];
 } pdosgpu_options;
 
 typedef struct {
@@ -202,6 +208,16 @@ int64_t pdosgpu_batch_done(pdosgpu_batch *b);
  * (128, 256, 512, 1024), keeps the fastest, resets the batch; blocks (may be
  * NULL) receives the choice for the five classes. */
 int pdosgpu_batch_tune(pdosgpu_batch *b, int iters, int *blocks);
+/* Layout autotuner: sets up batches of up to `sample` of the problems
+ * (evenly spaced) with each candidate layout -- long-row cut 64, 128 or
+ * 256 nonzeros, times pieces of 256, 512, 1,024 or 2,048 -- times `iters`
+ * rounds of their two CG products (the SpMV pair of linAlg.h:70-115) and
+ * returns the fastest pair in *long_row and *piece, for the options of the
+ * batch proper.  The layout changes only how each row's sum is split among
+ * warps, not the problems. */
+int pdosgpu_batch_tune_layout(const pdosgpu_problem *probs, int64_t count,
+                              const pdosgpu_options *opt, int64_t sample, int iters,
+                              int *long_row, int *piece);
 /* Roofline timing: the two CG products (u = A p, t = p + A'u) of every
  * instance, `reps` times, with nothing else; *ms = device time of the
  * launches, *bytes (may be NULL) = their algorithmic bytes (values and

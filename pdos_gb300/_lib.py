@@ -32,7 +32,8 @@ PDOSGPU_ENGINE_CTA = 2
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("scaling", c_int), ("device", c_int),
-                ("batch_layouts", c_int), ("engine", c_int), ("reserved", c_int * 3)]
+                ("batch_layouts", c_int), ("engine", c_int), ("batch_long_row", c_int),
+                ("batch_piece", c_int), ("reserved", c_int * 1)]
 
 
 class Info(ctypes.Structure):
@@ -103,6 +104,8 @@ SIGNATURES = {
     "pdosgpu_batch_tune": (c_int, [c_void_p, c_int, POINTER(c_int)]),
     "pdosgpu_batch_set_blocks": (c_int, [c_void_p, POINTER(c_int)]),
     "pdosgpu_batch_time_products": (c_int, [c_void_p, c_int, POINTER(c_double), POINTER(c_double)]),
+    "pdosgpu_batch_tune_layout": (c_int, [POINTER(Problem), c_int64, POINTER(Options), c_int64, c_int,
+                                          POINTER(c_int), POINTER(c_int)]),
     "pdosgpu_batch_sizes": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64),
                                     POINTER(c_int64), POINTER(c_int64)]),
     "pdosgpu_batch_stream": (c_void_p, [c_void_p]),

@@ -999,6 +999,12 @@ class BatchEngine : public BatchBase {
 
  private:
   int append_wave(const pdosgpu_problem *probs, int64_t cnt);
+  void layout_params(HybBuild &a, HybBuild &b) const {
+    for (HybBuild *h : {&a, &b}) {
+      if (opt_.batch_long_row > 0) h->long_row = opt_.batch_long_row;
+      if (opt_.batch_piece > 0) h->piece = opt_.batch_piece;
+    }
+  }
   int build_graph(int iter_cap, cudaGraphExec_t *exec);
   int configure(int cls, int block);
   int launch_class(int cls, int block, int iter_cap, cudaStream_t st);
@@ -1064,6 +1070,10 @@ int BatchEngine<T>::append(const pdosgpu_problem *probs, int64_t cnt) {
     return fail(PDOSGPU_ENOTSUP, "Ruiz equilibration is not available for batches");
   if (opt_.batch_layouts != PDOSGPU_BATCH_SHARE && opt_.batch_layouts != PDOSGPU_BATCH_OWN)
     return fail(PDOSGPU_EINVAL, "batch_layouts must be PDOSGPU_BATCH_SHARE or PDOSGPU_BATCH_OWN");
+  if (opt_.batch_long_row != 0 && (opt_.batch_long_row % 4 || opt_.batch_long_row < 4 || opt_.batch_long_row > 1024))
+    return fail(PDOSGPU_EINVAL, "batch_long_row must be 0 or a multiple of 4 in [4, 1024]");
+  if (opt_.batch_piece != 0 && (opt_.batch_piece % 4 || opt_.batch_piece < 64 || opt_.batch_piece > 16384))
+    return fail(PDOSGPU_EINVAL, "batch_piece must be 0 or a multiple of 4 in [64, 16384]");
   PDOS_CUDA_TRY(cudaSetDevice(opt_.device));
   size_t free_b = 0, total_b = 0;
   PDOS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -1254,6 +1264,7 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
       if (group_of[i] < 0) own.push_back(i);
     if (!own.empty()) {
       HybBuild bA, bT;
+      layout_params(bA, bT);
       std::vector<Side> sides;
       const int64_t no = (int64_t)own.size();
       build_layout<int32_t>(bA, no, [&](int64_t k, const int32_t *&ptr, const int32_t *&g, int64_t &r0,
@@ -1298,6 +1309,7 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
       for (int64_t k = pr.Ap[j]; k < pr.Ap[j + 1]; ++k) csr2csc[next[pr.Ai[k]]++] = k;
     const int64_t rbase = rp[wrow0[ref]], cbase = Ap[wcol0[ref]];
     HybBuild bA, bT;
+    layout_params(bA, bT);
     std::vector<Side> sA, sT;
     build_layout<int32_t>(bA, 1, [&](int64_t, const int32_t *&ptr, const int32_t *&g, int64_t &r0, int64_t &r1,
                                      int64_t &c0) {
@@ -1977,6 +1989,38 @@ int pdosgpu_batch_set_blocks(pdosgpu_batch *b, const int *blocks) {
   PDOS_TRY(ready(b));
   if (!blocks) return fail(PDOSGPU_EINVAL, "NULL argument");
   return b->engine->set_blocks(blocks);
+}
+
+int pdosgpu_batch_tune_layout(const pdosgpu_problem *probs, int64_t count, const pdosgpu_options *opt,
+                              int64_t sample, int iters, int *long_row, int *piece) {
+  if (!probs || !long_row || !piece) return fail(PDOSGPU_EINVAL, "NULL argument");
+  if (count <= 0 || sample <= 0 || iters <= 0) return fail(PDOSGPU_EINVAL, "count, sample and iters must be positive");
+  pdosgpu_options o;
+  pdosgpu_default_options(&o);
+  if (opt) o = *opt;
+  const int64_t ns = std::min(count, sample);
+  std::vector<pdosgpu_problem> pick(ns);
+  for (int64_t k = 0; k < ns; ++k) pick[k] = probs[ns == 1 ? 0 : k * (count - 1) / (ns - 1)];
+  const int rows[] = {64, 128, 256}, pieces[] = {256, 512, 1024, 2048};
+  double best = -1.0;
+  for (int lr : rows) {
+    for (int pc : pieces) {
+      o.batch_long_row = lr;
+      o.batch_piece = pc;
+      pdosgpu_batch *b = nullptr;
+      PDOS_TRY(pdosgpu_batch_setup(pick.data(), ns, &o, 0, &b));
+      double ms = 0.0;
+      int rc = b->engine->time_products(iters, &ms, nullptr);
+      delete b;
+      PDOS_TRY(rc);
+      if (best < 0.0 || ms < best) {
+        best = ms;
+        *long_row = lr;
+        *piece = pc;
+      }
+    }
+  }
+  return PDOSGPU_OK;
 }
 
 int pdosgpu_batch_sizes(pdosgpu_batch *b, int64_t *count, int64_t *n, int64_t *m, int64_t *nnz) {

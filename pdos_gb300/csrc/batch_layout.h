@@ -18,8 +18,8 @@ namespace batch {
 #ifndef PDOS_BATCH_PIECE
 #define PDOS_BATCH_PIECE 1024
 #endif
-constexpr int kLongRow = 128;               // rows with more nonzeros go to warp-wide pieces
-constexpr int kPiece = PDOS_BATCH_PIECE;    // target nonzeros per piece
+constexpr int kLongRow = 128;               // default: rows with more nonzeros go to warp-wide pieces
+constexpr int kPiece = PDOS_BATCH_PIECE;    // default target nonzeros per piece
 
 // One side (A: rows of A; At: rows of A', i.e. columns of A) of an instance
 // in the hybrid layout: slices of 32 consecutive rows stored column-major
@@ -73,6 +73,8 @@ struct Cursor {
 // the same decisions, and every instance starts and ends on a multiple of
 // 4 elements, so instances can be sized and written in parallel.
 struct HybBuild {
+  int long_row = kLongRow;  // rows with more nonzeros go to pieces (a multiple of 4, >= 4)
+  int piece = kPiece;       // nonzeros per piece at most (a multiple of 4, >= 4)
   std::vector<int64_t> slice_beg;
   std::vector<int32_t> slice_w;
   std::vector<uint32_t> slice_skip;
@@ -125,7 +127,7 @@ struct HybBuild {
           continue;
         }
         const int len = ptr[r0 + r + 1] - ptr[r0 + r];
-        if (len > kLongRow) {
+        if (len > long_row) {
           skip |= 1u << lane;
           continue;
         }
@@ -162,8 +164,8 @@ struct HybBuild {
     }
     for (int64_t r = 0; r < R; ++r) {
       const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
-      if (len <= kLongRow) continue;
-      const int64_t np = (len + kPiece - 1) / kPiece;
+      if (len <= long_row) continue;
+      const int64_t np = (len + piece - 1) / piece;
       if (np > 1) {
         if (WRITE) {
           split_row[c.split] = (int32_t)r;

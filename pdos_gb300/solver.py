@@ -24,7 +24,9 @@ _SCALING = {"2norm": _lib.PDOSGPU_SCALE_2NORM, "ruiz": _lib.PDOSGPU_SCALE_RUIZ}
 _ENGINE = {"auto": _lib.PDOSGPU_ENGINE_AUTO, "grid": _lib.PDOSGPU_ENGINE_GRID, "cta": _lib.PDOSGPU_ENGINE_CTA}
 
 
-def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True, engine="auto"):
+def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True, engine="auto",
+                 layout=None):
+    """Options of the C ABI; layout = (long_row, piece) of batch layouts, None for the defaults."""
     if precision not in _PRECISION:
         raise ValueError(f"precision must be one of {sorted(_PRECISION)}")
     if scaling not in _SCALING:
@@ -38,6 +40,8 @@ def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True
     if engine not in _ENGINE:
         raise ValueError(f"engine must be one of {sorted(_ENGINE)}")
     opt.engine = _ENGINE[engine]
+    if layout is not None:
+        opt.batch_long_row, opt.batch_piece = int(layout[0]), int(layout[1])
     return opt
 
 
@@ -181,14 +185,14 @@ class Batch:
     """Many independent problems solved together (pdosgpu_batch_*): one CTA
     per instance at a time, convergence masking, per-instance results."""
 
-    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0, share_layouts=True):
+    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0, share_layouts=True, layout=None):
         self.lib = _lib.load()
         probs = list(probs)
         self.probs = probs
         self.sizes = [(p.n, p.m) for p in probs]
         keep = []
         arr = _c_problems(probs, keep)
-        self._opt = make_options(precision, "2norm", device, share_layouts)
+        self._opt = make_options(precision, "2norm", device, share_layouts, layout=layout)
         self._b = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_batch_setup(arr, len(probs), ctypes.byref(self._opt),
                                                 int(iters_per_launch), ctypes.byref(self._b)),
@@ -196,7 +200,7 @@ class Batch:
         self._totals()
 
     @classmethod
-    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0, share_layouts=True):
+    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0, share_layouts=True, layout=None):
         """A batch set up from an iterable of problem lists, one
         pdosgpu_batch_append per list, so that only one list has to exist on
         the host at a time (pdosgpu_batch_create / append / commit).  Keeps
@@ -205,7 +209,7 @@ class Batch:
         self.lib = _lib.load()
         self.probs = None
         self.sizes = []
-        self._opt = make_options(precision, "2norm", device, share_layouts)
+        self._opt = make_options(precision, "2norm", device, share_layouts, layout=layout)
         self._b = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_batch_create(ctypes.byref(self._opt), int(iters_per_launch),
                                                  ctypes.byref(self._b)), "pdosgpu_batch_create", self.lib)
@@ -355,6 +359,20 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def tune_layout(probs, precision="fp64", device=0, sample=256, iters=4, share_layouts=True):
+    """The batch layout autotuner (pdosgpu_batch_tune_layout): the fastest
+    (long_row, piece) for these problems, timed on up to `sample` of them;
+    pass it as Batch(..., layout=...)."""
+    lib = _lib.load()
+    keep = []
+    arr = _c_problems(list(probs), keep)
+    opt = make_options(precision, "2norm", device, share_layouts)
+    lr, pc = ctypes.c_int(), ctypes.c_int()
+    _lib.check(lib.pdosgpu_batch_tune_layout(arr, len(probs), ctypes.byref(opt), int(sample), int(iters),
+                                             ctypes.byref(lr), ctypes.byref(pc)), "pdosgpu_batch_tune_layout", lib)
+    return lr.value, pc.value
 
 
 def pdos_batch_call(probs, precision=None, libname="libpdosindir.so"):

@@ -49,7 +49,13 @@ int main() {
     c0.push_back(c0.back() + n);
   }
 
+  // the default layout parameters and other values the layout tuner tries
+  const int params[][2] = {{kLongRow, kPiece}, {64, 256}, {256, 2048}, {32, 512}};
+  long long total_elems = 0;
+  for (const auto &lp : params) {
   HybBuild hb;
+  hb.long_row = lp[0];
+  hb.piece = lp[1];
   std::vector<Side> sides;
   build_layout<int32_t>(hb, count, [&](int64_t i, const int32_t *&p, const int32_t *&gi, int64_t &a, int64_t &b,
                                        int64_t &c) {
@@ -80,7 +86,7 @@ int main() {
       const int w = hb.slice_w[k];
       const int64_t beg = hb.slice_beg[k];
       if (w < 0) {
-        CHECK(-w % 4 == 0 && -w <= kLongRow, "instance %d slice %d: width %d", i, s, w);
+        CHECK(-w % 4 == 0 && -w <= hb.long_row, "instance %d slice %d: width %d", i, s, w);
         CHECK(beg % 4 == 0, "instance %d slice %d: start %lld not 4-aligned", i, s, (long long)beg);
       } else {
         CHECK(w < 4, "instance %d slice %d: narrow width %d", i, s, w);
@@ -94,7 +100,7 @@ int main() {
         if (r >= m) continue;
         seen[r]++;
         const int64_t a = ptr[r0[i] + r], len = ptr[r0[i] + r + 1] - a;
-        CHECK(len <= kLongRow, "instance %d: long row %lld in a slice", i, (long long)r);
+        CHECK(len <= hb.long_row, "instance %d: long row %lld in a slice", i, (long long)r);
         for (int c = 0; c < width; ++c) {  // entry c of the lane's row
           const int64_t e = w < 0 ? beg + 128LL * (c / 4) + 4 * lane + c % 4 : beg + 32LL * c + lane;
           if (c < len) {
@@ -109,14 +115,14 @@ int main() {
     for (int k = 0; k < sd.npieces; ++k) {
       const int64_t pk = sd.piece0 + k;
       const int len = hb.piece_len[pk];
-      CHECK(len % 4 == 0 && len > 0 && len <= kPiece, "instance %d piece %d: length %d", i, k, len);
+      CHECK(len % 4 == 0 && len > 0 && len <= hb.piece, "instance %d piece %d: length %d", i, k, len);
       CHECK(hb.piece_beg[pk] % 4 == 0, "instance %d piece %d: start not 4-aligned", i, k);
       const int32_t pr = hb.piece_row[pk];
       const int64_t r = pr >= 0 ? pr : ~pr;
       CHECK(r >= 0 && r < m, "instance %d piece %d: row %lld", i, k, (long long)r);
       if (r < 0 || r >= m) continue;
       const int64_t len_r = ptr[r0[i] + r + 1] - ptr[r0[i] + r];
-      CHECK(len_r > kLongRow, "instance %d: short row %lld in a piece", i, (long long)r);
+      CHECK(len_r > hb.long_row, "instance %d: short row %lld in a piece", i, (long long)r);
       if (pr >= 0) seen[r]++;  // a whole row in one piece
     }
     for (int k = 0; k < sd.nsplit; ++k) {
@@ -133,11 +139,13 @@ int main() {
     for (int64_t r = 0; r < m; ++r) CHECK(seen[r] == 1, "instance %d row %lld covered %d times", i, (long long)r, seen[r]);
   }
   CHECK(nsplit_total > 0, "no split rows were exercised");
+  total_elems += (long long)hb.idx.size();
+  }
   if (failures) {
     std::printf("%d failures\n", failures);
     return 1;
   }
-  std::printf("OK %d instances, %zu nonzeros, %lld layout elements, %lld split rows\n", count, col.size(),
-              (long long)hb.idx.size(), (long long)nsplit_total);
+  std::printf("OK %d instances, %zu nonzeros, %lld layout elements over %zu parameter sets\n", count, col.size(),
+              total_elems, sizeof(params) / sizeof(params[0]));
   return 0;
 }

@@ -358,3 +358,27 @@ def test_overflowing_instance_is_flagged_diverged_without_touching_neighbours(bu
     with Workspace(bad, "fp32") as w:
         r = w.solve().fetch()
     assert r["info"]["diverged"] == 1 and r["status"] == "Indeterminate" and r["iters"] <= 1
+
+
+def test_layout_autotuner_picks_a_candidate_and_layouts_agree(built_lib, torch_cuda):
+    """pdosgpu_batch_tune_layout returns one of its candidate (long-row cut,
+    piece length) pairs; batches laid out with the tuned and with an extreme
+    pair solve every instance to the same objectives (the layout only moves
+    where each row's sum is split), and a repeated solve of one layout is
+    bit-identical."""
+    from pdos_gb300.solver import Batch, tune_layout
+    probs = _uneven_portfolios()
+    lr, pc = tune_layout(probs, "fp32", sample=5, iters=2)
+    assert lr in (64, 128, 256) and pc in (256, 512, 1024, 2048)
+    with Batch(probs, precision="fp32", layout=(lr, pc)) as b:
+        tuned = b.solve().fetch()
+        again = b.reset().solve().fetch()
+    with Batch(probs, precision="fp32", layout=(32, 128)) as b:
+        other = b.solve().fetch()
+    for i, (p, u, v, w) in enumerate(zip(probs, tuned, other, again)):
+        assert u["status"] == v["status"] == "Solved", i
+        assert np.array_equal(u["x"], w["x"])
+        o_u, o_v = float(p.c @ u["x"]), float(p.c @ v["x"])
+        assert abs(o_u - o_v) <= 1e-3 * max(1.0, abs(o_v)), (i, o_u, o_v)
+    with pytest.raises(RuntimeError, match="batch_piece"):
+        Batch(probs[:1], precision="fp32", layout=(128, 6))
