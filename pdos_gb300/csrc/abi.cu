@@ -91,8 +91,11 @@ void set_status(Sol *sol, int solved) {
 // Nonzeros up to which pdos() solves a problem with one CTA of the batch
 // kernel: every ADMM iteration then runs inside one launch with CTA
 // barriers only, where the grid engine launches 2k + 4 kernels per
-// iteration (k CG steps) and waits on each.
-constexpr int64_t kOneCtaMaxNnz = 65536;
+// iteration (k CG steps) and waits on each.  Measured in FP64 on GB300
+// (solve time, set-up excluded): 2.7x faster on a 1,308-nonzero fixture,
+// 2.4x at 2,761 nonzeros, 1.3x at 23,201; at 86,401 the grid engine is
+// 2.3x faster, since one SM issues only about two FP64 FMAs per clock.
+constexpr int64_t kOneCtaMaxNnz = 32768;
 
 // pdos() through the one-CTA path: a batch of one instance, run to its stop
 // test in one launch of the persistent kernel (CTA size by size class).
