@@ -249,13 +249,28 @@ __device__ __forceinline__ void fma4(const Idx4 &j, const Val4<T> &v, const T *s
 // Split rows leave piece partials in pbuf and are finished after a barrier.
 // SHARED: the layout is a family group's; pv holds this instance's values
 // of the entries that vary within the group (see unbox).
-template <typename T, int BLOCK, int NV, bool SHARED, class Epi>
+// The work is split over the warps and threads that `Part` names -- one
+// CTA's, or a cluster's -- and `bar` orders the piece partials before the
+// split rows are finished (a CTA or a cluster barrier).
+struct Part {
+  int w0, ws;  // this warp's first piece / slice and the stride between warps
+  int t0, ts;  // this thread's first split row and the stride between threads
+};
+template <int BLOCK>
+__device__ __forceinline__ Part cta_part() {
+  return Part{(int)(threadIdx.x >> 5), BLOCK / 32, (int)threadIdx.x, BLOCK};
+}
+struct CtaBarrier {
+  __device__ void operator()() const { __syncthreads(); }
+};
+
+template <typename T, int NV, bool SHARED, class Bar, class Epi>
 __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd, const T *pv, const T *src0,
-                                                 const T *src1, T *pbuf, Epi &&epi) {
-  constexpr int W = BLOCK / 32;
+                                                 const T *src1, T *pbuf, const Part &pt, const Bar &bar,
+                                                 Epi &&epi) {
   const T *const hval = static_cast<const T *>(H.val);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int k = warp; k < sd.npieces; k += W) {
+  const int lane = threadIdx.x & 31;
+  for (int k = pt.w0; k < sd.npieces; k += pt.ws) {
     const int64_t pk = sd.piece0 + k;
     const int32_t prow = H.piece_row[pk];
     const int64_t beg = H.piece_beg[pk];
@@ -281,7 +296,7 @@ __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd
       }
     }
   }
-  for (int s = warp; s < sd.nslices; s += W) {
+  for (int s = pt.w0; s < sd.nslices; s += pt.ws) {
     const int64_t sk = sd.slice0 + s;
     const int64_t off = H.slice_beg[sk];
     const int width = H.slice_w[sk];
@@ -310,8 +325,8 @@ __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd
     if (!((H.slice_skip[sk] >> lane) & 1u)) epi(s * 32 + lane, a0, a1);
   }
   if (sd.nsplit > 0) {
-    __syncthreads();
-    for (int k = threadIdx.x; k < sd.nsplit; k += BLOCK) {
+    bar();
+    for (int k = pt.t0; k < sd.nsplit; k += pt.ts) {
       const int64_t sk = sd.split0 + k;
       const int p0 = H.split_p0[sk], np = H.split_np[sk];
       T a0 = T(0), a1 = T(0);
@@ -326,13 +341,19 @@ __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd
 
 // One product over one side of an instance, through its own layout or its
 // family group's shared one.
+template <typename T, int NV, class Bar, class Epi>
+__device__ __forceinline__ void hyb_product_part(const HybPtr &H, const Side &sd, const void *pv, const T *src0,
+                                                 const T *src1, T *pbuf, const Part &pt, const Bar &bar,
+                                                 Epi &&epi) {
+  if (pv)
+    hyb_product_impl<T, NV, true>(H, sd, static_cast<const T *>(pv), src0, src1, pbuf, pt, bar, epi);
+  else
+    hyb_product_impl<T, NV, false>(H, sd, nullptr, src0, src1, pbuf, pt, bar, epi);
+}
 template <typename T, int BLOCK, int NV, class Epi>
 __device__ __forceinline__ void hyb_product(const HybPtr &H, const Side &sd, const void *pv, const T *src0,
                                             const T *src1, T *pbuf, Epi &&epi) {
-  if (pv)
-    hyb_product_impl<T, BLOCK, NV, true>(H, sd, static_cast<const T *>(pv), src0, src1, pbuf, epi);
-  else
-    hyb_product_impl<T, BLOCK, NV, false>(H, sd, nullptr, src0, src1, pbuf, epi);
+  hyb_product_part<T, NV>(H, sd, pv, src0, src1, pbuf, cta_part<BLOCK>(), CtaBarrier{}, epi);
 }
 
 // Three-case SOC rule of cones.c:21-47 for one element.
@@ -684,6 +705,383 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev
 static_assert(sizeof(Inst) % 4 == 0 && sizeof(Inst) / 4 <= 128, "Inst is copied by one 128-thread pass");
 static_assert(alignof(Inst) == 8, "Inst is copied as 32-bit words into an 8-byte aligned slot");
 
+// ---------------------------------------------------------------- clusters
+// Large instances of the global-staging class run on a thread-block cluster
+// of kClusterCtas CTAs (one per SM): the warps of the whole cluster share
+// each product's pieces and slices, the element-wise loops are spread over
+// the cluster's threads, every CTA copies the vector a product gathers from
+// into its own shared memory, the staged vectors live in one global region
+// per cluster, and hardware cluster barriers (release / acquire at cluster
+// scope) order those global writes.  Block sums meet in CTA 0's shared
+// memory through distributed shared memory, in rank order, so every thread
+// of the cluster holds the same totals.  Per-row sums are those of the
+// one-CTA kernel; only the order of the block sums differs.
+constexpr int kClusterCtas = 8;  // portable cluster size
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Address of this CTA's shared variable `p` in the shared memory of CTA `rank`.
+__device__ __forceinline__ uint32_t dsmem_addr(const void *p, uint32_t rank) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_dsmem(uint32_t addr, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+}
+__device__ __forceinline__ double ld_dsmem(uint32_t addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_dsmem_i32(uint32_t addr) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+struct ClusterBarrier {
+  __device__ void operator()() const { cluster_sync(); }
+};
+
+// Cluster sums of N values: each CTA's block sum (block_sum_n), CTA r's
+// totals stored into slot r of CTA 0, a cluster barrier, then every warp
+// loads the C slots into its lanes and runs the xor butterfly -- the same
+// bits everywhere.  Two slot halves are used in turn, as in Reduce.
+template <int BLOCK, int C>
+struct ClusterReduce {
+  double *scratch;  // this CTA: 2 x 3 x BLOCK/32
+  double *slots;    // every CTA's copy; CTA 0's is the one used: 2 x 3 x C
+  uint32_t rank;
+  int half;
+  template <int N>
+  __device__ __forceinline__ void operator()(double (&v)[N]) {
+    half ^= 1;
+    block_sum_n<BLOCK, N>(v, scratch + half * 3 * (BLOCK / 32));
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) st_dsmem(dsmem_addr(&slots[(half * 3 + k) * C + rank], 0), v[k]);
+    }
+    cluster_sync();
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      v[k] = warp_sum(lane < C ? ld_dsmem(dsmem_addr(&slots[(half * 3 + k) * C + lane], 0)) : 0.0);
+  }
+};
+
+// One instance on a cluster (global staging, gathers from each CTA's shared
+// memory): the operations and their order are those of solve_instance with
+// SG; rows are shared among the cluster's warps and element-wise loops
+// among its threads.
+template <typename T, int BLOCK, int C>
+__device__ void solve_instance_cluster(const Dev<T> &B, const Inst &I, State *gst, int iter_cap, T *g1, T *g2,
+                                       T *tt, T *pbuf, double *scratch, double *slots, T *gs, uint32_t rank) {
+  constexpr int W = BLOCK / 32, CT = C * BLOCK;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int ct = (int)rank * BLOCK + tid;  // thread index in the cluster
+  const Part part{(int)rank * W + warp, C * W, ct, CT};
+  const ClusterBarrier cbar;
+  const int m = I.m, n = I.n, f = I.f, l = I.l;
+  T *__restrict__ x = B.x + I.col0;
+  T *__restrict__ q = B.q + I.col0;
+  T *__restrict__ s = B.s + I.row0;
+  T *__restrict__ y = B.y + I.row0;
+  T *__restrict__ st = B.st + I.row0;
+  T *__restrict__ u = B.u + I.row0;
+  T *__restrict__ ax = B.ax + I.row0;
+  const T *__restrict__ b = B.b + I.row0;
+  const T *__restrict__ D = B.D + I.row0;
+  const T *__restrict__ c = B.c + I.col0;
+  const T *__restrict__ E = B.E + I.col0;
+  const T lam = (T)I.lambda;
+  const T alpha = (T)I.alpha, oma = (T)(1.0 - I.alpha);
+
+  State S = *gst;  // the same in every thread of the cluster
+  if (S.done) return;
+  ClusterReduce<BLOCK, C> reduce{scratch, slots, rank, 0};
+
+  auto finish = [&](int r, T sv, T stv, T axv, double &pr2, double &byv) {
+    const T yv = y[r] + (sv - stv) / lam;
+    y[r] = yv;
+    s[r] = sv;
+    const T bv = b[r];
+    const T pr = ((sv - bv) + axv) / D[r];
+    pr2 += (double)pr * (double)pr;
+    u[r] = ((sv + lam * yv) - bv) + axv;
+    byv += (double)bv * (double)yv;
+  };
+  // every CTA copies a complete vector (ordered by an earlier cluster
+  // barrier) into its own shared memory
+  auto to_gs = [&](const T *src, int len) {
+    for (int j = tid; j < len; j += BLOCK) gs[j] = src[j];
+    __syncthreads();
+  };
+
+  if (!S.prepped) {  // A x0: residual, u and b'y of iteration 0
+    to_gs(x, n);
+    double red[2] = {0.0, 0.0};
+    hyb_product_part<T, 1>(I.hA, I.A, I.pvA, gs, gs, pbuf, part, cbar, [&](int r, T a, T) {
+      ax[r] = a;
+      const T sv = s[r], bv = b[r], yv = y[r];
+      const T pr = ((sv - bv) + a) / D[r];
+      red[0] += (double)pr * (double)pr;
+      u[r] = ((sv + lam * yv) - bv) + a;
+      red[1] += (double)bv * (double)yv;
+    });
+    reduce(red);
+    S.pres_sq = red[0];
+    S.by = red[1];
+    S.prepped = 1;
+  }
+
+  bool newly_done = false;
+  for (int it = 0; it < iter_cap; ++it) {
+    // ---- top: A'y into tt, then A'u with the epilogue (dual residual,
+    // c'x, CG start); the same thread handles row j in both passes
+    to_gs(y, m);
+    hyb_product_part<T, 1>(I.hT, I.At, I.pvT, gs, gs, pbuf, part, cbar, [&](int j, T sy, T) { tt[j] = sy; });
+    cluster_sync();  // every CTA has read the piece partials before the next product rewrites them
+    to_gs(u, m);
+    double top[3] = {0.0, 0.0, 0.0};
+    hyb_product_part<T, 1>(I.hT, I.At, I.pvT, gs, gs, pbuf, part, cbar, [&](int j, T su, T) {
+      const T cj = c[j];
+      const T dr = (cj + tt[j]) / E[j];
+      top[0] += (double)dr * (double)dr;
+      top[1] += (double)cj * (double)x[j];
+      const T qj = (-lam) * cj + (-su);
+      q[j] = qj;
+      top[2] += (double)qj * (double)qj;
+    });
+    reduce(top);
+    S.p_res = sqrt(S.pres_sq);
+    S.d_res = sqrt(top[0]);
+    S.p_obj = top[1];
+    S.d_obj = -S.by;
+    S.eta = fabs(S.p_obj - S.d_obj);
+    if (S.p_res < I.eps * I.pscale && S.d_res < I.eps * I.dscale &&
+        S.eta < I.eps * (1.0 + fabs(S.p_obj) + fabs(S.d_obj))) {
+      S.solved = 1;
+      S.done = 1;
+      newly_done = true;
+      break;
+    }
+    if (!isfinite(S.p_res) || !isfinite(S.d_res) || !isfinite(S.eta)) {
+      S.diverged = 1;
+      S.done = 1;
+      newly_done = true;
+      break;
+    }
+    // ---- CG (indirect/private.c:31-104)
+    double qsold = top[2];
+    int cg_iter = 0;
+    bool active = I.cg_max > 0 && qsold > I.tol_sq;
+    if (active) {
+      for (int j = ct; j < n; j += CT) g1[j] = q[j];  // p = q
+      cluster_sync();
+      to_gs(g1, n);
+    }
+    while (active) {
+      hyb_product_part<T, 1>(I.hA, I.A, I.pvA, gs, gs, pbuf, part, cbar, [&](int r, T a, T) { g2[r] = a; });
+      cluster_sync();  // A p complete, every gather from p done
+      to_gs(g2, m);
+      double pt[1] = {0.0};
+      hyb_product_part<T, 1>(I.hT, I.At, I.pvT, gs, gs, pbuf, part, cbar, [&](int j, T a, T) {
+        const T pj = g1[j];
+        const T tj = pj + a;
+        tt[j] = tj;
+        pt[0] += (double)pj * (double)tj;
+      });
+      reduce(pt);
+      const double step = qsold / pt[0];
+      const T stp = (T)step, nstp = (T)(-step);
+      double qs[1] = {0.0};
+      for (int j = ct; j < n; j += CT) {
+        x[j] = x[j] + stp * g1[j];
+        const T qj = q[j] + nstp * tt[j];
+        q[j] = qj;
+        qs[0] += (double)qj * (double)qj;
+      }
+      reduce(qs);
+      ++cg_iter;
+      ++S.cg_total;
+      double ratio = 0.0;
+      if (qs[0] < I.tol_sq) {
+        active = false;
+      } else {
+        ratio = qs[0] / qsold;
+        qsold = qs[0];
+        if (cg_iter >= I.cg_max) active = false;
+      }
+      if (active) {
+        const T beta = (T)ratio;
+        for (int j = ct; j < n; j += CT) g1[j] = beta * g1[j] + q[j];
+        cluster_sync();
+        to_gs(g1, n);
+      }
+    }
+    // ---- A x: s~ = b - Ax, relax, s = s~ - lam y; zero / orthant rows done
+    cluster_sync();  // x complete and every gather of the CG products done
+    to_gs(x, n);
+    double fin[2] = {0.0, 0.0};
+    hyb_product_part<T, 1>(I.hA, I.A, I.pvA, gs, gs, pbuf, part, cbar, [&](int r, T a, T) {
+      T stv = b[r] + (-a);
+      stv = alpha * stv + oma * s[r];
+      T v = stv - lam * y[r];
+      ax[r] = a;
+      if (r < f) {
+        finish(r, T(0), stv, a, fin[0], fin[1]);
+      } else if (r < f + l) {
+        if (v < T(0)) v = T(0);
+        finish(r, v, stv, a, fin[0], fin[1]);
+      } else {
+        s[r] = v;
+        st[r] = stv;
+      }
+    });
+    cluster_sync();  // s and s~ of every cone row complete
+    // ---- second-order cones: a warp per small cone, the cluster per big one
+    {
+      const int lane = tid & 31;
+      for (int k = part.w0; k < I.ncones; k += part.ws) {
+        const int off = B.cone_off[I.cone0 + k], len = B.cone_len[I.cone0 + k];
+        if (len > kSmallCone) continue;
+        T acc = T(0);
+        for (int i = 1 + lane; i < len; i += 32) {
+          const T v = s[off + i];
+          acc += v * v;
+        }
+        acc = warp_sum_t(acc);
+        const T tail = sqrt(acc);
+        const T head = s[off];
+        __syncwarp();
+        for (int i = lane; i < len; i += 32) {
+          const int r = off + i;
+          finish(r, soc_rule(s[r], i == 0, head, tail), st[r], ax[r], fin[0], fin[1]);
+        }
+      }
+      for (int k = 0; k < I.ncones; ++k) {  // uniform over the cluster
+        const int off = B.cone_off[I.cone0 + k], len = B.cone_len[I.cone0 + k];
+        if (len <= kSmallCone) continue;
+        const T head = s[off];  // read before any thread rewrites the cone
+        double acc[1] = {0.0};
+        for (int i = 1 + ct; i < len; i += CT) {
+          const T v = s[off + i];
+          acc[0] += (double)(v * v);
+        }
+        reduce(acc);
+        const T tail = (T)sqrt(acc[0]);
+        for (int i = ct; i < len; i += CT) {
+          const int r = off + i;
+          finish(r, soc_rule(s[r], i == 0, head, tail), st[r], ax[r], fin[0], fin[1]);
+        }
+      }
+    }
+    reduce(fin);
+    S.pres_sq = fin[0];
+    S.by = fin[1];
+    S.admm_iter += 1;
+    if (S.admm_iter >= I.max_iters) {
+      S.done = 1;
+      newly_done = true;
+      break;
+    }
+  }
+  cluster_sync();
+  if (rank == 0 && tid == 0) {
+    *gst = S;
+    if (newly_done) atomicAdd(B.ndone, 1);
+  }
+}
+
+// The next instance of the class for the whole cluster: CTA 0 takes it from
+// the queue and every CTA reads CTA 0's copy; the second barrier keeps CTA 0
+// from overwriting it before everyone has read it.
+__device__ __forceinline__ int cluster_next(int *queue, int *s_k, uint32_t rank) {
+  if (rank == 0 && threadIdx.x == 0) *s_k = atomicAdd(queue, 1);
+  cluster_sync();
+  const int k = ld_dsmem_i32(dsmem_addr(s_k, 0));
+  cluster_sync();
+  return k;
+}
+
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1) batch_cluster_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
+  constexpr int C = kClusterCtas;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double scratch[2 * 3 * (BLOCK / 32)];
+  __shared__ double slots[2 * 3 * C];
+  __shared__ Inst s_inst;
+  __shared__ int s_k;
+  const uint32_t rank = cluster_rank();
+  T *gs = reinterpret_cast<T *>(smem_raw);
+  T *g1 = B.gscratch + (size_t)(blockIdx.x / C) * sm.stride();
+  T *g2 = g1 + sm.g1;
+  T *tt = g2 + sm.g2;
+  T *pbuf = tt + sm.tt;
+  const int begin = B.class_begin[cls], count = B.class_begin[cls + 1] - begin;
+  for (;;) {
+    const int k = cluster_next(&B.queue[cls], &s_k, rank);
+    if (k >= count) break;  // the same k in every CTA of the cluster
+    const int id = B.order[begin + k];
+    if (threadIdx.x < (int)(sizeof(Inst) / 4))
+      reinterpret_cast<int32_t *>(&s_inst)[threadIdx.x] = reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
+    __syncthreads();
+    solve_instance_cluster<T, BLOCK, C>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch, slots, gs,
+                                        rank);
+  }
+  cluster_sync();  // no CTA leaves while another may still read its shared memory
+}
+
+// The two CG products alone on clusters (roofline timing of that class).
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1) batch_cluster_products_kernel(Dev<T> B, int cls, Smem sm, int reps) {
+  constexpr int C = kClusterCtas, W = BLOCK / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Inst s_inst;
+  __shared__ int s_k;
+  const uint32_t rank = cluster_rank();
+  T *gs = reinterpret_cast<T *>(smem_raw);
+  T *g1 = B.gscratch + (size_t)(blockIdx.x / C) * sm.stride();
+  T *g2 = g1 + sm.g1;
+  T *tt = g2 + sm.g2;
+  T *pbuf = tt + sm.tt;
+  const Part part{(int)rank * W + (int)(threadIdx.x >> 5), C * W, (int)rank * BLOCK + (int)threadIdx.x, C * BLOCK};
+  const ClusterBarrier cbar;
+  const int begin = B.class_begin[cls], count = B.class_begin[cls + 1] - begin;
+  for (;;) {
+    const int k = cluster_next(&B.queue[cls], &s_k, rank);
+    if (k >= count) break;
+    const int id = B.order[begin + k];
+    if (threadIdx.x < (int)(sizeof(Inst) / 4))
+      reinterpret_cast<int32_t *>(&s_inst)[threadIdx.x] = reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
+    __syncthreads();
+    const Inst &I = s_inst;
+    const T *x = B.x + I.col0;
+    for (int j = part.t0; j < I.n; j += part.ts) g1[j] = x[j];
+    cluster_sync();
+    for (int r = 0; r < reps; ++r) {
+      for (int j = threadIdx.x; j < I.n; j += BLOCK) gs[j] = g1[j];
+      __syncthreads();
+      hyb_product_part<T, 1>(I.hA, I.A, I.pvA, gs, gs, pbuf, part, cbar, [&](int row, T a, T) { g2[row] = a; });
+      cluster_sync();
+      for (int j = threadIdx.x; j < I.m; j += BLOCK) gs[j] = g2[j];
+      __syncthreads();
+      hyb_product_part<T, 1>(I.hT, I.At, I.pvT, gs, gs, pbuf, part, cbar,
+                             [&](int j, T a, T) { tt[j] = g1[j] + a; });
+      cluster_sync();
+    }
+  }
+  cluster_sync();
+}
+
 // y = D y-unscale etc. (pdos.c:261-294) over the stacked vectors.
 template <typename T>
 __global__ void unscale_kernel(const T *x, const T *s, const T *y, const double *D, const double *E,
@@ -822,6 +1220,55 @@ KernelOf<T> products_kernel_mode(int block) {
 }
 inline int stage_mode(const Smem &sm) {
   return !sm.global ? kStageShared : (sm.gs > 0 ? kStageGlobalSG : kStageGlobal);
+}
+// A global-staging class whose gather vectors fit shared memory runs on
+// clusters of kClusterCtas CTAs, one instance per cluster.
+inline bool on_clusters(const Smem &sm) { return stage_mode(sm) == kStageGlobalSG; }
+template <typename T>
+KernelOf<T> cluster_kernel_for(int block, bool products) {
+  switch (block) {
+    case 128: return products ? batch_cluster_products_kernel<T, 128> : batch_cluster_kernel<T, 128>;
+    case 256: return products ? batch_cluster_products_kernel<T, 256> : batch_cluster_kernel<T, 256>;
+    case 512: return products ? batch_cluster_products_kernel<T, 512> : batch_cluster_kernel<T, 512>;
+    case 1024: return products ? batch_cluster_products_kernel<T, 1024> : batch_cluster_kernel<T, 1024>;
+    default: return nullptr;
+  }
+}
+inline cudaLaunchConfig_t cluster_config(int grid, int block, size_t bytes, cudaStream_t st,
+                                         cudaLaunchAttribute *attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kClusterCtas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+// Grid (a multiple of kClusterCtas) of a cluster kernel: as many clusters as
+// fit the device at once, at most one per instance and per staging region.
+template <typename T>
+int cluster_grid(KernelOf<T> kernel, int block, size_t bytes, int members, int regions, int *grid) {
+  PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config(kClusterCtas, block, bytes, nullptr, attr);
+  int nc = 0;
+  PDOS_CUDA_TRY(cudaOccupancyMaxActiveClusters(&nc, (const void *)kernel, &cfg));
+  if (nc < 1) return fail(PDOSGPU_ENOTSUP, "a cluster of the batch kernel does not fit the device");
+  *grid = std::max(1, std::min(std::min(members, nc), regions)) * kClusterCtas;
+  return PDOSGPU_OK;
+}
+template <typename T>
+int launch_clusters(KernelOf<T> kernel, int grid, int block, size_t bytes, cudaStream_t st, const Dev<T> &dev,
+                    int cls, const Smem &sm, int arg) {
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config(grid, block, bytes, st, attr);
+  PDOS_CUDA_TRY(cudaLaunchKernelEx(&cfg, kernel, dev, cls, sm, arg));
+  return PDOSGPU_OK;
 }
 template <typename T>
 KernelOf<T> admm_kernel_for(int block, const Smem &sm) {
@@ -1525,9 +1972,10 @@ int BatchEngine<T>::commit() {
   B.cone_off = cone_off_d;
   B.cone_len = cone_len_d;
   B.gscratch = nullptr;
-  {  // one staging region per resident CTA of the global class (at most 8 per SM)
+  {  // one staging region per resident CTA (at most 8 per SM) or cluster of the global class
     const int members_g = class_begin_h_[kGlobalClass + 1] - class_begin_h_[kGlobalClass];
-    gregions_ = std::min(members_g, num_sms() * (1024 / kBlocks[0]));
+    gregions_ = on_clusters(smem_[kGlobalClass]) ? std::min(members_g, std::max(1, num_sms() / kClusterCtas))
+                                                 : std::min(members_g, num_sms() * (1024 / kBlocks[0]));
     if (gregions_ > 0) PDOS_TRY(arena_.alloc(&B.gscratch, (size_t)gregions_ * smem_[kGlobalClass].stride()));
   }
   PDOS_TRY(arena_.alloc(&out_, (size_t)N + 2 * (size_t)M));
@@ -1572,6 +2020,12 @@ int BatchEngine<T>::configure(int cls, int block) {
     if (smem_[cls].global) grid_[cls] = std::min(grid_[cls], gregions_);
     return PDOSGPU_OK;
   };
+  const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
+  if (on_clusters(smem_[cls])) {
+    auto kernel = cluster_kernel_for<T>(block, false);
+    if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+    return cluster_grid<T>(kernel, block, bytes, members, gregions_, &grid_[cls]);
+  }
   auto kernel = admm_kernel_for<T>(block, smem_[cls]);
   if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
   return go(kernel);
@@ -1581,6 +2035,11 @@ template <typename T>
 int BatchEngine<T>::launch_class(int cls, int block, int iter_cap, cudaStream_t st) {
   const Smem sm = smem_[cls];
   const size_t bytes = sm.bytes(sizeof(T));
+  if (on_clusters(sm)) {
+    auto kernel = cluster_kernel_for<T>(block, false);
+    if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+    return launch_clusters<T>(kernel, grid_[cls], block, bytes, st, dev_, cls, sm, iter_cap);
+  }
   auto kernel = admm_kernel_for<T>(block, sm);
   if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
   kernel<<<grid_[cls], block, bytes, st>>>(dev_, cls, sm, iter_cap);
@@ -1826,6 +2285,13 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
   }
   auto go = [&](int cls, int block, auto kernel) -> int {
     const size_t sm_bytes = smem_[cls].bytes(sizeof(T));
+    if (on_clusters(smem_[cls])) {
+      auto ck = cluster_kernel_for<T>(block, true);
+      if (!ck) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
+      int grid = 0;
+      PDOS_TRY(cluster_grid<T>(ck, block, sm_bytes, class_begin_h_[cls + 1] - class_begin_h_[cls], gregions_, &grid));
+      return launch_clusters<T>(ck, grid, block, sm_bytes, st, dev_, cls, smem_[cls], reps);
+    }
     PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
     int per_sm = 0;
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, sm_bytes));

@@ -382,3 +382,42 @@ def test_layout_autotuner_picks_a_candidate_and_layouts_agree(built_lib, torch_c
         assert abs(o_u - o_v) <= 1e-3 * max(1.0, abs(o_v)), (i, o_u, o_v)
     with pytest.raises(RuntimeError, match="batch_piece"):
         Batch(probs[:1], precision="fp32", layout=(128, 6))
+
+
+def _cluster_batch():
+    """Portfolios whose vectors exceed one CTA's shared memory but whose
+    gather vector fits it (the global-staging class on clusters), between
+    ordinary instances."""
+    from pdos_gb300 import generators as g
+    P = dict(EPS_ABS=1e-4, VERBOSE=0, MAX_ITERS=3000)
+    return [g.portfolio(100, 10, 0.5, seed=15, params=P),
+            g.portfolio(11000, 1100, 0.02, seed=16, params=P),
+            g.portfolio(300, 30, 0.2, seed=17, params=P),
+            g.portfolio(12000, 240, 0.05, seed=18, params=P, random_soc_split=True)]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_large_instances_on_clusters_match_single_instance_solves(built_lib, torch_cuda, precision):
+    """Instances of the global-staging class run on 8-CTA clusters (rows
+    shared among the cluster's warps, sums met through distributed shared
+    memory); each must match its single-instance solve as the one-CTA batch
+    does, and a repeated solve must give the same bits."""
+    from pdos_gb300.solver import Batch, solve_problem
+    probs = _cluster_batch()
+    with Batch(probs, precision=precision) as b:
+        classes = b.classes()
+        outs = b.solve().fetch()
+        again = b.reset().solve().fetch()
+    assert classes[1] == classes[3] == 4 and classes[0] < 4 and classes[2] < 4, classes
+    obj_tol = 1e-5 if precision == "fp64" else 1e-3
+    for i, (p, out, rep) in enumerate(zip(probs, outs, again)):
+        assert np.array_equal(out["x"], rep["x"]) and out["iters"] == rep["iters"], i
+        single = solve_problem(p, precision)
+        assert out["status"] == single["status"] == "Solved", i
+        o_b, o_s = float(p.c @ out["x"]), float(p.c @ single["x"])
+        assert abs(o_b - o_s) <= obj_tol * max(1.0, abs(o_s)), (i, o_b, o_s)
+        if precision == "fp64":
+            assert abs(out["iters"] - single["iters"]) <= max(3, 0.02 * single["iters"]), \
+                (i, out["iters"], single["iters"])
+            for k in ("x", "s", "y"):
+                assert rel(out[k], single[k]) <= 1e-4, (i, k, rel(out[k], single[k]))
