@@ -224,6 +224,19 @@ template <typename T>
 __device__ __forceinline__ T unbox(T v, const T *pv) {
   return v != v ? __ldg(pv + box_payload(v)) : v;
 }
+// Four loaded values with their boxes resolved.  FP32: one NaN test of the
+// values' sum finds any box (a NaN propagates through the sum; input data is
+// finite, so anything else is an overflowed sum, which the per-value test
+// then leaves alone) -- three adds and a compare per four values instead of
+// four compares and selects.  FP64 keeps the per-value test, as FP64 adds
+// are scarce.
+__device__ __forceinline__ void unbox4(Val4<float> &v, const float *pv) {
+  const float probe = (v.x + v.y) + (v.z + v.w);
+  if (probe != probe) v = Val4<float>{unbox(v.x, pv), unbox(v.y, pv), unbox(v.z, pv), unbox(v.w, pv)};
+}
+__device__ __forceinline__ void unbox4(Val4<double> &v, const double *pv) {
+  v = Val4<double>{unbox(v.x, pv), unbox(v.y, pv), unbox(v.z, pv), unbox(v.w, pv)};
+}
 
 // Four consecutive entries of one row into the NV running sums, in order.
 template <typename T, int NV>
@@ -282,7 +295,7 @@ __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd
     for (int e = 4 * lane; e < len; e += 128) {
       const Idx4 j = ld_stream4(ip + e);
       Val4<T> v = ld_stream4(vp + e);
-      if (SHARED) v = Val4<T>{unbox(v.x, pv), unbox(v.y, pv), unbox(v.z, pv), unbox(v.w, pv)};
+      if (SHARED) unbox4(v, pv);
       fma4<T, NV>(j, v, src0, src1, a0, a1);
     }
     a0 = warp_sum_t(a0);
@@ -308,7 +321,7 @@ __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd
       for (int c4 = 0; c4 < -width; c4 += 4) {
         const Idx4 j = ld_stream4(ip + 32 * c4);
         Val4<T> v = ld_stream4(vp + 32 * c4);
-        if (SHARED) v = Val4<T>{unbox(v.x, pv), unbox(v.y, pv), unbox(v.z, pv), unbox(v.w, pv)};
+        if (SHARED) unbox4(v, pv);
         fma4<T, NV>(j, v, src0, src1, a0, a1);
       }
     } else {
@@ -1249,11 +1262,27 @@ inline cudaLaunchConfig_t cluster_config(int grid, int block, size_t bytes, cuda
   cfg.numAttrs = 1;
   return cfg;
 }
+// Lets `kernel` take as much dynamic shared memory as the device allows a
+// block beside the kernel's own static shared memory; PDOSGPU_ENOTSUP when
+// `need` bytes do not fit (a CTA size the tuner then skips).
+template <typename K>
+int allow_dynamic_smem(K kernel, size_t need) {
+  cudaFuncAttributes a{};
+  PDOS_CUDA_TRY(cudaFuncGetAttributes(&a, (const void *)kernel));
+  int dev = 0, optin = 0;
+  PDOS_CUDA_TRY(cudaGetDevice(&dev));
+  PDOS_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t room = (size_t)optin > a.sharedSizeBytes ? (size_t)optin - a.sharedSizeBytes : 0;
+  if (need > room) return fail(PDOSGPU_ENOTSUP, "the batch kernel's shared memory does not fit at this CTA size");
+  PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room));
+  return PDOSGPU_OK;
+}
+
 // Grid (a multiple of kClusterCtas) of a cluster kernel: as many clusters as
 // fit the device at once, at most one per instance and per staging region.
 template <typename T>
 int cluster_grid(KernelOf<T> kernel, int block, size_t bytes, int members, int regions, int *grid) {
-  PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
+  PDOS_TRY(allow_dynamic_smem(kernel, bytes));
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = cluster_config(kClusterCtas, block, bytes, nullptr, attr);
   int nc = 0;
@@ -2011,7 +2040,7 @@ int BatchEngine<T>::configure(int cls, int block) {
   const size_t bytes = smem_[cls].bytes(sizeof(T));
   auto go = [&](auto kernel) -> int {
     // one limit for every class that shares this kernel
-    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
+    PDOS_TRY(allow_dynamic_smem(kernel, bytes));
     int per_sm = 0;
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, bytes));
     if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "batch kernel does not fit on an SM");
@@ -2232,6 +2261,10 @@ int BatchEngine<T>::tune(int iters, int *blocks_out) {
       if (smem_[k].bytes(sizeof(T)) > (size_t)kSmemLimit) continue;
       rc = reset();
       if (rc == PDOSGPU_OK) rc = configure(k, blk);
+      if (rc == PDOSGPU_ENOTSUP) {  // this CTA size does not fit the class's shared memory
+        rc = PDOSGPU_OK;
+        continue;
+      }
       if (rc != PDOSGPU_OK) break;
       // prepare (first pass) outside the timed region
       if (cudaMemsetAsync(queue_, 0, sizeof(int32_t) * kClasses, st) != cudaSuccess) {
@@ -2292,7 +2325,7 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
       PDOS_TRY(cluster_grid<T>(ck, block, sm_bytes, class_begin_h_[cls + 1] - class_begin_h_[cls], gregions_, &grid));
       return launch_clusters<T>(ck, grid, block, sm_bytes, st, dev_, cls, smem_[cls], reps);
     }
-    PDOS_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
+    PDOS_TRY(allow_dynamic_smem(kernel, sm_bytes));
     int per_sm = 0;
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, sm_bytes));
     if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "product kernel does not fit on an SM");

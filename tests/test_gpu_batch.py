@@ -406,6 +406,8 @@ def test_large_instances_on_clusters_match_single_instance_solves(built_lib, tor
     probs = _cluster_batch()
     with Batch(probs, precision=precision) as b:
         classes = b.classes()
+        blocks = b.tune(iters=2)  # every CTA size that fits, clusters included
+        assert all(v in (128, 256, 512, 1024) for v in blocks)
         outs = b.solve().fetch()
         again = b.reset().solve().fetch()
     assert classes[1] == classes[3] == 4 and classes[0] < 4 and classes[2] < 4, classes
