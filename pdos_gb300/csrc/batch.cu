@@ -112,11 +112,12 @@ struct Dev {
 // gather from shared memory, larger ones from their global region.
 struct Smem {
   int32_t g1, g2, tt, pb, global, gs;
+  int32_t pair;  // shared-memory class run as pairs of family instances: twice the regions
   __host__ __device__ size_t stride() const {  // elements per CTA region, 128-byte multiples
     return ((size_t)g1 + g2 + tt + pb + 31) & ~(size_t)31;
   }
   size_t need(size_t elem) const { return elem * ((size_t)g1 + g2 + tt + pb); }
-  size_t bytes(size_t elem) const { return global ? elem * (size_t)gs : need(elem); }
+  size_t bytes(size_t elem) const { return global ? elem * (size_t)gs : (pair ? 2 : 1) * need(elem); }
 };
 
 // Base of a CTA's staging regions.  A compile-time choice, so that kernels
@@ -162,14 +163,15 @@ __device__ __forceinline__ void block_sum_n(double (&v)[N], double *scratch) {
 }
 
 // Two scratch halves of 3 * BLOCK/32 doubles, used in turn.
-template <int BLOCK>
+template <int BLOCK, int MAXN = 3>
 struct Reduce {
-  double *scratch;
+  double *scratch;  // 2 x MAXN x BLOCK/32
   int half;
   template <int N>
   __device__ __forceinline__ void operator()(double (&v)[N]) {
+    static_assert(N <= MAXN, "scratch too small");
     half ^= 1;
-    block_sum_n<BLOCK, N>(v, scratch + half * 3 * (BLOCK / 32));
+    block_sum_n<BLOCK, N>(v, scratch + half * MAXN * (BLOCK / 32));
   }
 };
 
@@ -717,6 +719,525 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_products_kernel(Dev
 
 static_assert(sizeof(Inst) % 4 == 0 && sizeof(Inst) / 4 <= 128, "Inst is copied by one 128-thread pass");
 static_assert(alignof(Inst) == 8, "Inst is copied as 32-bit words into an 8-byte aligned slot");
+
+// ------------------------------------------------------------------ pairs
+// Two instances of one family group (one shared layout, the same sizes and
+// cones) solved together by one CTA: every streamed load of the shared
+// layout serves both, their vectors sit interleaved in shared memory so one
+// 8-byte (FP32) gather feeds both FMA chains, and each instance keeps its
+// own per-row sums, in the order of the one-instance kernel, and its own
+// block sums -- so each result is bit for bit the one-instance result.  The
+// two run in lockstep; an instance that stops (or an empty second slot)
+// keeps flowing through the products with its writes masked.
+template <typename T>
+struct alignas(2 * sizeof(T)) P2 {
+  T a, b;
+};
+
+template <typename T>
+__device__ __forceinline__ P2<T> warp_sum_p(P2<T> v) {
+  return P2<T>{warp_sum_t(v.a), warp_sum_t(v.b)};
+}
+
+template <typename T, int NV>
+__device__ __forceinline__ void fma4_pair(const Idx4 &j, const Val4<T> &v0, const Val4<T> &v1, const P2<T> *s0,
+                                          const P2<T> *s1, P2<T> &a0, P2<T> &a1) {
+  const int jj[4] = {j.x, j.y, j.z, j.w};
+  const T w0[4] = {v0.x, v0.y, v0.z, v0.w}, w1[4] = {v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const P2<T> g = s0[jj[e]];
+    a0.a = fma(w0[e], g.a, a0.a);
+    a0.b = fma(w1[e], g.b, a0.b);
+    if (NV == 2) {
+      const P2<T> h = s1[jj[e]];
+      a1.a = fma(w0[e], h.a, a1.a);
+      a1.b = fma(w1[e], h.b, a1.b);
+    }
+  }
+}
+
+// The values of four loaded entries for each of the two instances: the
+// shared ones, or each instance's own where a NaN box marks a varying entry.
+template <typename T>
+__device__ __forceinline__ void unbox4_pair(const Val4<T> &v, const T *pv0, const T *pv1, Val4<T> &v0,
+                                            Val4<T> &v1) {
+  v0 = v;
+  v1 = v;
+  unbox4(v0, pv0);
+  unbox4(v1, pv1);
+}
+
+// One product over one side, for both instances of a pair; epi(row, s0, s1)
+// gets each source vector's pair of sums.
+template <typename T, int BLOCK, int NV, class Epi>
+__device__ __forceinline__ void pair_product(const HybPtr &H, const Side &sd, const T *pv0, const T *pv1,
+                                             const P2<T> *src0, const P2<T> *src1, P2<T> *pbuf, Epi &&epi) {
+  constexpr int W = BLOCK / 32;
+  const T *const hval = static_cast<const T *>(H.val);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = warp; k < sd.npieces; k += W) {
+    const int64_t pk = sd.piece0 + k;
+    const int32_t prow = H.piece_row[pk];
+    const int64_t beg = H.piece_beg[pk];
+    const int len = H.piece_len[pk];
+    P2<T> a0{T(0), T(0)}, a1{T(0), T(0)};
+    const uint16_t *ip = H.idx + beg;
+    const T *vp = hval + beg;
+#pragma unroll kUnroll
+    for (int e = 4 * lane; e < len; e += 128) {
+      const Idx4 j = ld_stream4(ip + e);
+      Val4<T> v0, v1;
+      unbox4_pair(ld_stream4(vp + e), pv0, pv1, v0, v1);
+      fma4_pair<T, NV>(j, v0, v1, src0, src1, a0, a1);
+    }
+    a0 = warp_sum_p(a0);
+    if (NV == 2) a1 = warp_sum_p(a1);
+    if (lane == 0) {
+      if (prow >= 0) {
+        epi(prow, a0, a1);
+      } else {
+        pbuf[k * NV] = a0;
+        if (NV == 2) pbuf[k * NV + 1] = a1;
+      }
+    }
+  }
+  for (int s = warp; s < sd.nslices; s += W) {
+    const int64_t sk = sd.slice0 + s;
+    const int64_t off = H.slice_beg[sk];
+    const int width = H.slice_w[sk];
+    P2<T> a0{T(0), T(0)}, a1{T(0), T(0)};
+    if (width < 0) {
+      const uint16_t *ip = H.idx + off + 4 * lane;
+      const T *vp = hval + off + 4 * lane;
+#pragma unroll kUnroll
+      for (int c4 = 0; c4 < -width; c4 += 4) {
+        const Idx4 j = ld_stream4(ip + 32 * c4);
+        Val4<T> v0, v1;
+        unbox4_pair(ld_stream4(vp + 32 * c4), pv0, pv1, v0, v1);
+        fma4_pair<T, NV>(j, v0, v1, src0, src1, a0, a1);
+      }
+    } else {
+      const uint16_t *ip = H.idx + off + lane;
+      const T *vp = hval + off + lane;
+      for (int c = 0; c < width; ++c) {
+        const int j = ip[c * 32];
+        const T v = vp[c * 32];
+        const T v0 = unbox(v, pv0), v1 = unbox(v, pv1);
+        const P2<T> g = src0[j];
+        a0.a = fma(v0, g.a, a0.a);
+        a0.b = fma(v1, g.b, a0.b);
+        if (NV == 2) {
+          const P2<T> h = src1[j];
+          a1.a = fma(v0, h.a, a1.a);
+          a1.b = fma(v1, h.b, a1.b);
+        }
+      }
+    }
+    if (!((H.slice_skip[sk] >> lane) & 1u)) epi(s * 32 + lane, a0, a1);
+  }
+  if (sd.nsplit > 0) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < sd.nsplit; k += BLOCK) {
+      const int64_t sk = sd.split0 + k;
+      const int p0 = H.split_p0[sk], np = H.split_np[sk];
+      P2<T> a0{T(0), T(0)}, a1{T(0), T(0)};
+      for (int t = 0; t < np; ++t) {
+        const P2<T> u0 = pbuf[(p0 + t) * NV];
+        a0.a += u0.a;
+        a0.b += u0.b;
+        if (NV == 2) {
+          const P2<T> u1 = pbuf[(p0 + t) * NV + 1];
+          a1.a += u1.a;
+          a1.b += u1.b;
+        }
+      }
+      epi(H.split_row[sk], a0, a1);
+    }
+  }
+}
+
+// Per-instance pointers of one slot of a pair.
+template <typename T>
+struct Slot {
+  T *x, *q, *s, *y, *st, *u, *ax;
+  const T *b, *c, *D, *E;
+  T lam, alpha, oma;
+};
+
+template <typename T, int BLOCK>
+__device__ void solve_pair(const Dev<T> &B, const Inst *I2, State *gst0, State *gst1, int iter_cap, P2<T> *g1,
+                           P2<T> *g2, P2<T> *tt, P2<T> *pbuf, double *scratch) {
+  const int tid = threadIdx.x;
+  const Inst &I = I2[0];  // layout, sizes and cones of both
+  const int m = I.m, n = I.n, f = I.f, l = I.l;
+  const bool two = gst1 != nullptr;
+  Slot<T> sl[2];
+#pragma unroll
+  for (int g = 0; g < 2; ++g) {
+    const Inst &J = I2[g];
+    sl[g] = Slot<T>{B.x + J.col0, B.q + J.col0, B.s + J.row0, B.y + J.row0, B.st + J.row0, B.u + J.row0,
+                    B.ax + J.row0, B.b + J.row0, B.c + J.col0, B.D + J.row0, B.E + J.col0, (T)J.lambda,
+                    (T)J.alpha, (T)(1.0 - J.alpha)};
+  }
+  const T *pvA0 = static_cast<const T *>(I2[0].pvA), *pvA1 = static_cast<const T *>(I2[1].pvA);
+  const T *pvT0 = static_cast<const T *>(I2[0].pvT), *pvT1 = static_cast<const T *>(I2[1].pvT);
+  State S[2] = {*gst0, two ? *gst1 : *gst0};
+  bool act[2] = {!S[0].done, two && !S[1].done};  // instances still iterating
+  bool newly[2] = {false, false};
+  if (!act[0] && !act[1]) return;
+  Reduce<BLOCK, 6> reduce{scratch, 0};
+
+  // dual update and next residual inputs of one row of slot g (pdos.c:232-236,
+  // linAlg.h:158-175, indirect/private.c:20-29, :58-60)
+  auto finish = [&](int g, int r, T sv, T stv, T axv, double &pr2, double &byv) {
+    const Slot<T> &z = sl[g];
+    const T yv = z.y[r] + (sv - stv) / z.lam;
+    z.y[r] = yv;
+    z.s[r] = sv;
+    const T bv = z.b[r];
+    const T pr = ((sv - bv) + axv) / z.D[r];
+    pr2 += (double)pr * (double)pr;
+    z.u[r] = ((sv + z.lam * yv) - bv) + axv;
+    byv += (double)bv * (double)yv;
+  };
+  // interleaved copy of one vector of both slots into a pair array
+  auto stage = [&](P2<T> *dst, int len, T *const Slot<T>::*field) {
+    for (int j = tid; j < len; j += BLOCK) dst[j] = P2<T>{(sl[0].*field)[j], (sl[1].*field)[j]};
+  };
+
+  if (!S[0].prepped || (two && !S[1].prepped)) {  // A x0 of each slot not yet prepared
+    stage(g1, n, &Slot<T>::x);
+    __syncthreads();
+    double red[4] = {0.0, 0.0, 0.0, 0.0};
+    pair_product<T, BLOCK, 1>(I.hA, I.A, pvA0, pvA1, g1, g1, pbuf, [&](int r, P2<T> a, P2<T>) {
+      const T av[2] = {a.a, a.b};
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        if (!act[g] || S[g].prepped) continue;
+        const Slot<T> &z = sl[g];
+        z.ax[r] = av[g];
+        const T sv = z.s[r], bv = z.b[r], yv = z.y[r];
+        const T pr = ((sv - bv) + av[g]) / z.D[r];
+        red[2 * g] += (double)pr * (double)pr;
+        z.u[r] = ((sv + z.lam * yv) - bv) + av[g];
+        red[2 * g + 1] += (double)bv * (double)yv;
+      }
+    });
+    reduce(red);
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      if (!act[g] || S[g].prepped) continue;
+      S[g].pres_sq = red[2 * g];
+      S[g].by = red[2 * g + 1];
+      S[g].prepped = 1;
+    }
+  }
+
+  for (int it = 0; it < iter_cap && (act[0] || act[1]); ++it) {
+    // ---- top: A' on (y, u): dual residual, c'x, CG start; stop test
+    for (int r = tid; r < m; r += BLOCK) {
+      g1[r] = P2<T>{sl[0].y[r], sl[1].y[r]};
+      g2[r] = P2<T>{sl[0].u[r], sl[1].u[r]};
+    }
+    __syncthreads();
+    double top[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    pair_product<T, BLOCK, 2>(I.hT, I.At, pvT0, pvT1, g1, g2, pbuf, [&](int j, P2<T> sy, P2<T> su) {
+      const T syv[2] = {sy.a, sy.b}, suv[2] = {su.a, su.b};
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        if (!act[g]) continue;
+        const Slot<T> &z = sl[g];
+        const T cj = z.c[j];
+        const T dr = (cj + syv[g]) / z.E[j];
+        top[3 * g] += (double)dr * (double)dr;
+        top[3 * g + 1] += (double)cj * (double)z.x[j];
+        const T qj = (-z.lam) * cj + (-suv[g]);
+        z.q[j] = qj;
+        top[3 * g + 2] += (double)qj * (double)qj;
+      }
+    });
+    reduce(top);
+    double qsold[2] = {top[2], top[5]};
+    int cg_iter[2] = {0, 0};
+    bool cg_on[2] = {false, false};
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      if (!act[g]) continue;
+      const Inst &J = I2[g];
+      State &Z = S[g];
+      Z.p_res = sqrt(Z.pres_sq);
+      Z.d_res = sqrt(top[3 * g]);
+      Z.p_obj = top[3 * g + 1];
+      Z.d_obj = -Z.by;
+      Z.eta = fabs(Z.p_obj - Z.d_obj);
+      if (Z.p_res < J.eps * J.pscale && Z.d_res < J.eps * J.dscale &&
+          Z.eta < J.eps * (1.0 + fabs(Z.p_obj) + fabs(Z.d_obj))) {
+        Z.solved = 1;
+        Z.done = 1;
+        newly[g] = true;
+        act[g] = false;
+      } else if (!isfinite(Z.p_res) || !isfinite(Z.d_res) || !isfinite(Z.eta)) {
+        Z.diverged = 1;
+        Z.done = 1;
+        newly[g] = true;
+        act[g] = false;
+      } else {
+        cg_on[g] = J.cg_max > 0 && qsold[g] > J.tol_sq;
+      }
+    }
+    if (!act[0] && !act[1]) break;
+    // ---- CG on (I + A'A) x = ... warm-started at x (indirect/private.c:31-104)
+    if (cg_on[0] || cg_on[1]) {
+      for (int j = tid; j < n; j += BLOCK) {  // p = q (a finished slot keeps its p)
+        P2<T> pj = g1[j];
+        if (cg_on[0]) pj.a = sl[0].q[j];
+        if (cg_on[1]) pj.b = sl[1].q[j];
+        g1[j] = pj;
+      }
+      __syncthreads();
+    }
+    while (cg_on[0] || cg_on[1]) {
+      pair_product<T, BLOCK, 1>(I.hA, I.A, pvA0, pvA1, g1, g1, pbuf, [&](int r, P2<T> a, P2<T>) { g2[r] = a; });
+      __syncthreads();
+      double pt[2] = {0.0, 0.0};
+      pair_product<T, BLOCK, 1>(I.hT, I.At, pvT0, pvT1, g2, g2, pbuf, [&](int j, P2<T> a, P2<T>) {
+        const P2<T> pj = g1[j];
+        const P2<T> tj{pj.a + a.a, pj.b + a.b};
+        tt[j] = tj;
+        pt[0] += (double)pj.a * (double)tj.a;
+        pt[1] += (double)pj.b * (double)tj.b;
+      });
+      reduce(pt);
+      T stp[2], nstp[2];
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const double step = cg_on[g] ? qsold[g] / pt[g] : 0.0;
+        stp[g] = (T)step;
+        nstp[g] = (T)(-step);
+      }
+      double qs[2] = {0.0, 0.0};
+#pragma unroll 2
+      for (int j = tid; j < n; j += BLOCK) {
+        const P2<T> pj = g1[j], tj = tt[j];
+        if (cg_on[0]) {
+          sl[0].x[j] = sl[0].x[j] + stp[0] * pj.a;
+          const T qj = sl[0].q[j] + nstp[0] * tj.a;
+          sl[0].q[j] = qj;
+          qs[0] += (double)qj * (double)qj;
+        }
+        if (cg_on[1]) {
+          sl[1].x[j] = sl[1].x[j] + stp[1] * pj.b;
+          const T qj = sl[1].q[j] + nstp[1] * tj.b;
+          sl[1].q[j] = qj;
+          qs[1] += (double)qj * (double)qj;
+        }
+      }
+      reduce(qs);
+      T beta[2] = {T(0), T(0)};
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        if (!cg_on[g]) continue;
+        ++cg_iter[g];
+        ++S[g].cg_total;
+        if (qs[g] < I2[g].tol_sq) {
+          cg_on[g] = false;
+        } else {
+          beta[g] = (T)(qs[g] / qsold[g]);
+          qsold[g] = qs[g];
+          if (cg_iter[g] >= I2[g].cg_max) cg_on[g] = false;
+        }
+      }
+      if (cg_on[0] || cg_on[1]) {
+#pragma unroll 2
+        for (int j = tid; j < n; j += BLOCK) {
+          P2<T> pj = g1[j];
+          if (cg_on[0]) pj.a = beta[0] * pj.a + sl[0].q[j];
+          if (cg_on[1]) pj.b = beta[1] * pj.b + sl[1].q[j];
+          g1[j] = pj;
+        }
+        __syncthreads();
+      }
+    }
+    // ---- A x: s~ = b - Ax, relax, s = s~ - lam y; zero / orthant rows done
+    stage(g1, n, &Slot<T>::x);
+    __syncthreads();
+    double fin[4] = {0.0, 0.0, 0.0, 0.0};
+    pair_product<T, BLOCK, 1>(I.hA, I.A, pvA0, pvA1, g1, g1, pbuf, [&](int r, P2<T> a, P2<T>) {
+      const T av[2] = {a.a, a.b};
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        if (!act[g]) continue;
+        const Slot<T> &z = sl[g];
+        T stv = z.b[r] + (-av[g]);
+        stv = z.alpha * stv + z.oma * z.s[r];
+        T v = stv - z.lam * z.y[r];
+        z.ax[r] = av[g];
+        if (r < f) {
+          finish(g, r, T(0), stv, av[g], fin[2 * g], fin[2 * g + 1]);
+        } else if (r < f + l) {
+          if (v < T(0)) v = T(0);
+          finish(g, r, v, stv, av[g], fin[2 * g], fin[2 * g + 1]);
+        } else {
+          z.s[r] = v;
+          z.st[r] = stv;
+        }
+      }
+    });
+    __syncthreads();
+    // ---- second-order cones: a warp per small cone, the CTA per big cone
+    {
+      const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        if (!act[g]) continue;
+        const Slot<T> &z = sl[g];
+        for (int k = warp; k < I.ncones; k += BLOCK / 32) {
+          const int off = B.cone_off[I.cone0 + k], len = B.cone_len[I.cone0 + k];
+          if (len > kSmallCone) continue;
+          T acc = T(0);
+          for (int i = 1 + lane; i < len; i += 32) {
+            const T v = z.s[off + i];
+            acc += v * v;
+          }
+          acc = warp_sum_t(acc);
+          const T tail = sqrt(acc);
+          const T head = z.s[off];
+          __syncwarp();
+          for (int i = lane; i < len; i += 32) {
+            const int r = off + i;
+            finish(g, r, soc_rule(z.s[r], i == 0, head, tail), z.st[r], z.ax[r], fin[2 * g], fin[2 * g + 1]);
+          }
+        }
+      }
+      for (int k = 0; k < I.ncones; ++k) {  // uniform over the CTA
+        const int off = B.cone_off[I.cone0 + k], len = B.cone_len[I.cone0 + k];
+        if (len <= kSmallCone) continue;
+        T head[2];
+        double acc[2] = {0.0, 0.0};
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          head[g] = sl[g].s[off];  // read before any thread rewrites the cone
+          if (!act[g]) continue;
+          for (int i = 1 + tid; i < len; i += BLOCK) {
+            const T v = sl[g].s[off + i];
+            acc[g] += (double)(v * v);
+          }
+        }
+        reduce(acc);
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          if (!act[g]) continue;
+          const Slot<T> &z = sl[g];
+          const T tail = (T)sqrt(acc[g]);
+          for (int i = tid; i < len; i += BLOCK) {
+            const int r = off + i;
+            finish(g, r, soc_rule(z.s[r], i == 0, head[g], tail), z.st[r], z.ax[r], fin[2 * g], fin[2 * g + 1]);
+          }
+        }
+      }
+    }
+    reduce(fin);
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      if (!act[g]) continue;
+      S[g].pres_sq = fin[2 * g];
+      S[g].by = fin[2 * g + 1];
+      S[g].admm_iter += 1;
+      if (S[g].admm_iter >= I2[g].max_iters) {
+        S[g].done = 1;
+        newly[g] = true;
+        act[g] = false;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    *gst0 = S[0];
+    if (newly[0]) atomicAdd(B.ndone, 1);
+    if (two) {
+      *gst1 = S[1];
+      if (newly[1]) atomicAdd(B.ndone, 1);
+    }
+  }
+}
+
+// The persistent kernel of a class whose work items are pairs of one family
+// group (order[2k], order[2k+1]; -1 for an empty second slot).  Its shared
+// memory holds the staging regions of two instances, interleaved.
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double scratch[2 * 6 * (BLOCK / 32)];
+  __shared__ Inst s_inst[2];
+  __shared__ int s_k;
+  P2<T> *g1 = reinterpret_cast<P2<T> *>(smem_raw);
+  P2<T> *g2 = g1 + sm.g1;
+  P2<T> *tt = g2 + sm.g2;
+  P2<T> *pbuf = tt + sm.tt;
+  const int begin = B.class_begin[cls], items = (B.class_begin[cls + 1] - begin) / 2;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_k = atomicAdd(&B.queue[cls], 1);
+    __syncthreads();
+    const int k = s_k;
+    if (k >= items) break;
+    const int id0 = B.order[begin + 2 * k], id1 = B.order[begin + 2 * k + 1];
+    constexpr int kWords = (int)(sizeof(Inst) / 4);
+    for (int t = threadIdx.x; t < 2 * kWords; t += BLOCK) {
+      const int g = t / kWords, w = t % kWords;
+      const int id = (g == 1 && id1 >= 0) ? id1 : id0;
+      reinterpret_cast<int32_t *>(&s_inst[g])[w] = reinterpret_cast<const int32_t *>(B.inst + id)[w];
+    }
+    __syncthreads();
+    solve_pair<T, BLOCK>(B, s_inst, B.state + id0, id1 >= 0 ? B.state + id1 : nullptr, iter_cap, g1, g2, tt, pbuf,
+                         scratch);
+  }
+}
+
+// The two CG products alone for a paired class (roofline timing).
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_products_kernel(Dev<T> B, int cls, Smem sm,
+                                                                                   int reps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Inst s_inst[2];
+  __shared__ int s_k;
+  P2<T> *g1 = reinterpret_cast<P2<T> *>(smem_raw);
+  P2<T> *g2 = g1 + sm.g1;
+  P2<T> *tt = g2 + sm.g2;
+  P2<T> *pbuf = tt + sm.tt;
+  const int begin = B.class_begin[cls], items = (B.class_begin[cls + 1] - begin) / 2;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_k = atomicAdd(&B.queue[cls], 1);
+    __syncthreads();
+    const int k = s_k;
+    if (k >= items) break;
+    const int id0 = B.order[begin + 2 * k], id1 = B.order[begin + 2 * k + 1];
+    constexpr int kWords = (int)(sizeof(Inst) / 4);
+    for (int t = threadIdx.x; t < 2 * kWords; t += BLOCK) {
+      const int g = t / kWords, w = t % kWords;
+      const int id = (g == 1 && id1 >= 0) ? id1 : id0;
+      reinterpret_cast<int32_t *>(&s_inst[g])[w] = reinterpret_cast<const int32_t *>(B.inst + id)[w];
+    }
+    __syncthreads();
+    const Inst &I = s_inst[0];
+    const T *x0 = B.x + s_inst[0].col0, *x1 = B.x + s_inst[1].col0;
+    const T *pvA0 = static_cast<const T *>(s_inst[0].pvA), *pvA1 = static_cast<const T *>(s_inst[1].pvA);
+    const T *pvT0 = static_cast<const T *>(s_inst[0].pvT), *pvT1 = static_cast<const T *>(s_inst[1].pvT);
+    for (int j = threadIdx.x; j < I.n; j += BLOCK) g1[j] = P2<T>{x0[j], x1[j]};
+    __syncthreads();
+    for (int r = 0; r < reps; ++r) {
+      pair_product<T, BLOCK, 1>(I.hA, I.A, pvA0, pvA1, g1, g1, pbuf, [&](int row, P2<T> a, P2<T>) { g2[row] = a; });
+      __syncthreads();
+      pair_product<T, BLOCK, 1>(I.hT, I.At, pvT0, pvT1, g2, g2, pbuf, [&](int j, P2<T> a, P2<T>) {
+        const P2<T> pj = g1[j];
+        tt[j] = P2<T>{pj.a + a.a, pj.b + a.b};
+      });
+      __syncthreads();
+    }
+  }
+}
 
 // ---------------------------------------------------------------- clusters
 // Large instances of the global-staging class run on a thread-block cluster
@@ -1300,7 +1821,18 @@ int launch_clusters(KernelOf<T> kernel, int grid, int block, size_t bytes, cudaS
   return PDOSGPU_OK;
 }
 template <typename T>
+KernelOf<T> pair_kernel_for(int block, bool products) {
+  switch (block) {
+    case 128: return products ? batch_pair_products_kernel<T, 128> : batch_pair_kernel<T, 128>;
+    case 256: return products ? batch_pair_products_kernel<T, 256> : batch_pair_kernel<T, 256>;
+    case 512: return products ? batch_pair_products_kernel<T, 512> : batch_pair_kernel<T, 512>;
+    case 1024: return products ? batch_pair_products_kernel<T, 1024> : batch_pair_kernel<T, 1024>;
+    default: return nullptr;
+  }
+}
+template <typename T>
 KernelOf<T> admm_kernel_for(int block, const Smem &sm) {
+  if (sm.pair) return pair_kernel_for<T>(block, false);
   switch (stage_mode(sm)) {
     case kStageShared: return admm_kernel_mode<T, kStageShared>(block);
     case kStageGlobalSG: return admm_kernel_mode<T, kStageGlobalSG>(block);
@@ -1309,6 +1841,7 @@ KernelOf<T> admm_kernel_for(int block, const Smem &sm) {
 }
 template <typename T>
 KernelOf<T> products_kernel_for(int block, const Smem &sm) {
+  if (sm.pair) return pair_kernel_for<T>(block, true);
   switch (stage_mode(sm)) {
     case kStageShared: return products_kernel_mode<T, kStageShared>(block);
     case kStageGlobalSG: return products_kernel_mode<T, kStageGlobalSG>(block);
@@ -1875,7 +2408,7 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
   auto r4 = [](int32_t v) { return (v + 3) & ~3; };
   for (int64_t i = 0; i < cnt; ++i) {
     Inst &I = inst_h_[first + i];
-    const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0, 0};
+    const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0, 0, 0};
     if (own.need(sizeof(T)) > (size_t)kSmemLimit) I.cls = kGlobalClass;
   }
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // the wave's set-up arrays are released next
@@ -1946,8 +2479,12 @@ int BatchEngine<T>::commit() {
   class_begin_h_.assign(kClasses + 1, 0);
   for (int k = 0; k < kClasses; ++k) {
     auto &mv = members[k];
-    std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) { return nnz_h_[a] > nnz_h_[bb]; });
-    Smem sm{0, 0, 0, 0, k == kGlobalClass ? 1 : 0, 0};
+    // largest first; a family group's instances (one layout) kept together
+    std::stable_sort(mv.begin(), mv.end(), [&](int32_t a, int32_t bb) {
+      if (nnz_h_[a] != nnz_h_[bb]) return nnz_h_[a] > nnz_h_[bb];
+      return std::less<const void *>()(inst_h_[a].hA.val, inst_h_[bb].hA.val);
+    });
+    Smem sm{0, 0, 0, 0, k == kGlobalClass ? 1 : 0, 0, 0};
     const int32_t gs_cap = (int32_t)(kSmemLimit / sizeof(T)) & ~3;  // gather vector in shared memory
     for (int32_t i : mv) {
       const Inst &I = inst_h_[i];
@@ -1958,10 +2495,32 @@ int BatchEngine<T>::commit() {
       if (sm.global) sm.gs = std::max(sm.gs, r4(std::max(I.m, I.n)));
     }
     if (sm.gs > gs_cap) sm.gs = 0;  // some member's vectors do not fit: gathers from global memory
-    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb), sm.global, sm.gs};
+    sm = Smem{r4(sm.g1), r4(sm.g2), r4(sm.tt), r4(sm.pb), sm.global, sm.gs, 0};
+    // pairs: consecutive members (the order keeps a group's instances together,
+    // all of one size) that share a family layout, when two instances' regions
+    // fit one CTA's shared memory
+    std::vector<int32_t> items;
+    if (!sm.global && 2 * sm.need(sizeof(T)) <= (size_t)kSmemLimit) {
+      int npairs = 0;
+      for (size_t a = 0; a < mv.size();) {
+        const Inst &A = inst_h_[mv[a]];
+        if (a + 1 < mv.size() && A.pvA != nullptr && inst_h_[mv[a + 1]].hA.val == A.hA.val) {
+          items.push_back(mv[a]);
+          items.push_back(mv[a + 1]);
+          ++npairs;
+          a += 2;
+        } else {
+          items.push_back(mv[a]);
+          items.push_back(-1);
+          a += 1;
+        }
+      }
+      if (npairs > 0) sm.pair = 1;
+    }
     smem_[k] = sm;
     block_[k] = k == 0 ? 128 : (k == 1 ? 256 : 512);
-    order.insert(order.end(), mv.begin(), mv.end());
+    if (sm.pair) order.insert(order.end(), items.begin(), items.end());
+    else order.insert(order.end(), mv.begin(), mv.end());
     class_begin_h_[k + 1] = (int32_t)order.size();
   }
 
@@ -2045,7 +2604,8 @@ int BatchEngine<T>::configure(int cls, int block) {
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, bytes));
     if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "batch kernel does not fit on an SM");
     const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
-    grid_[cls] = std::max(1, std::min(members, per_sm * num_sms()));
+    const int work = smem_[cls].pair ? members / 2 : members;  // work items: pairs or instances
+    grid_[cls] = std::max(1, std::min(work, per_sm * num_sms()));
     if (smem_[cls].global) grid_[cls] = std::min(grid_[cls], gregions_);
     return PDOSGPU_OK;
   };
@@ -2330,7 +2890,8 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
     PDOS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, sm_bytes));
     if (per_sm < 1) return fail(PDOSGPU_ENOTSUP, "product kernel does not fit on an SM");
     const int members = class_begin_h_[cls + 1] - class_begin_h_[cls];
-    int grid = std::max(1, std::min(members, per_sm * num_sms()));
+    const int work = smem_[cls].pair ? members / 2 : members;
+    int grid = std::max(1, std::min(work, per_sm * num_sms()));
     if (smem_[cls].global) grid = std::min(grid, gregions_);
     kernel<<<grid, block, sm_bytes, st>>>(dev_, cls, smem_[cls], reps);
     PDOS_CUDA_TRY(cudaGetLastError());
