@@ -28,7 +28,7 @@ enum {
 enum { PDOSGPU_FP64 = 0, PDOSGPU_FP32 = 1 };          /* storage/arithmetic */
 enum { PDOSGPU_SCALE_2NORM = 0, PDOSGPU_SCALE_RUIZ = 1 }; /* NORMALIZE=1 kind */
 enum { PDOSGPU_BATCH_SHARE = 0, PDOSGPU_BATCH_OWN = 1 };  /* batch layouts */
-enum { PDOSGPU_ENGINE_AUTO = 0, PDOSGPU_ENGINE_GRID = 1, PDOSGPU_ENGINE_CTA = 2 };
+enum { PDOSGPU_ENGINE_AUTO = 0, PDOSGPU_ENGINE_GRID = 1, PDOSGPU_ENGINE_CTA = 2, PDOSGPU_ENGINE_CLUSTER = 3 };
 
 typedef struct {
   int precision;   /* PDOSGPU_FP64 (default): every operation in double, the
@@ -47,18 +47,23 @@ typedef struct {
                         the entries that differ (same results, bit for bit);
                         PDOSGPU_BATCH_OWN gives every instance its own */
   int engine;      /* pdos() / pdos_ex() only: PDOSGPU_ENGINE_AUTO (default)
-                      solves a small problem (m, n < 65,536, few nonzeros,
-                      VERBOSE=0, 2-norm scaling) in one launch of the batch
-                      kernel, one CTA running the whole ADMM loop, and any
-                      other on the grid engine; PDOSGPU_ENGINE_GRID and
-                      PDOSGPU_ENGINE_CTA force one of the two */
+                      solves a small problem (m, n < 65,536, VERBOSE=0,
+                      2-norm scaling) in one launch of the batch kernel --
+                      one CTA running the whole ADMM loop for the smallest,
+                      a cluster of 8 CTAs for mid-sized ones -- and any
+                      other on the grid engine; PDOSGPU_ENGINE_GRID,
+                      PDOSGPU_ENGINE_CTA and PDOSGPU_ENGINE_CLUSTER force
+                      one of the three */
   int batch_long_row; /* batches only: rows with more nonzeros than this are
                          cut into warp-wide pieces, shorter ones share
                          32-row slices (0: 128; else a multiple of 4 in
                          [4, 1024]) */
   int batch_piece;    /* batches only: nonzeros per piece at most (0: 1,024;
                          else a multiple of 4 in [64, 16384]) */
-  int reserved[1];
+  int batch_clusters; /* batches only: 0 (default) runs on 8-CTA clusters only
+                         the instances too large for one CTA's shared memory;
+                         1 runs every instance whose gather vector fits
+                         shared memory on a cluster */
 } pdosgpu_options;
 
 typedef struct {

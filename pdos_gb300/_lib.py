@@ -28,12 +28,13 @@ PDOSGPU_BATCH_OWN = 1
 PDOSGPU_ENGINE_AUTO = 0
 PDOSGPU_ENGINE_GRID = 1
 PDOSGPU_ENGINE_CTA = 2
+PDOSGPU_ENGINE_CLUSTER = 3
 
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int), ("scaling", c_int), ("device", c_int),
                 ("batch_layouts", c_int), ("engine", c_int), ("batch_long_row", c_int),
-                ("batch_piece", c_int), ("reserved", c_int * 1)]
+                ("batch_piece", c_int), ("batch_clusters", c_int)]
 
 
 class Info(ctypes.Structure):

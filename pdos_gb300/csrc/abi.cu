@@ -1,6 +1,7 @@
 // The reference's three entry points (pdos.h:85-87) on top of the C-ABI
 // layer.  Compiled once with PDOS_DLONG (idxint = long, libpdosindir.so) and
 // once without (idxint = int, libpdosindir_i32.so).
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -99,9 +100,14 @@ constexpr int64_t kOneCtaMaxNnz = 32768;
 
 // pdos() through the one-CTA path: a batch of one instance, run to its stop
 // test in one launch of the persistent kernel (CTA size by size class).
-Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_options *opt, pdosgpu_info *info) {
+Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_options *opt, pdosgpu_info *info,
+                   bool cluster) {
+  pdosgpu_options o;
+  pdosgpu_default_options(&o);
+  if (opt) o = *opt;
+  o.batch_clusters = cluster ? 1 : 0;
   pdosgpu_batch *b = NULL;
-  if (pdosgpu_batch_setup(&pr, 1, opt, 0, &b) != PDOSGPU_OK) return NULL;
+  if (pdosgpu_batch_setup(&pr, 1, &o, 0, &b) != PDOSGPU_OK) return NULL;
   Sol *sol = NULL;
   pdosgpu_info inf;
   if (pdosgpu_batch_solve(b) == PDOSGPU_OK) {
@@ -117,13 +123,24 @@ Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_optio
   return sol;
 }
 
-bool use_one_cta(const pdosgpu_problem &pr, const pdosgpu_options *opt) {
+// Nonzeros up to which pdos() solves on one 8-CTA cluster (above
+// kOneCtaMaxNnz); its gather vector must fit one CTA's shared memory.
+constexpr int64_t kClusterMaxNnz = 0;
+
+// 0: grid engine, 1: one CTA, 2: one cluster.
+int pick_engine(const pdosgpu_problem &pr, const pdosgpu_options *opt) {
   const int engine = opt ? opt->engine : PDOSGPU_ENGINE_AUTO;
-  if (engine == PDOSGPU_ENGINE_GRID) return false;
+  if (engine == PDOSGPU_ENGINE_GRID) return 0;
   const bool fits = pr.m <= 65535 && pr.n <= 65535 && !pr.verbose &&
                     !(pr.normalize && opt && opt->scaling == PDOSGPU_SCALE_RUIZ);
-  if (engine == PDOSGPU_ENGINE_CTA) return fits;
-  return fits && pr.Ap[pr.n] <= kOneCtaMaxNnz;
+  const size_t elem = (opt && opt->precision == PDOSGPU_FP32) ? 4 : 8;
+  const bool gather_fits = (size_t)std::max(pr.m, pr.n) * elem <= (size_t)225 * 1024;
+  if (engine == PDOSGPU_ENGINE_CTA) return fits ? 1 : 0;
+  if (engine == PDOSGPU_ENGINE_CLUSTER) return fits && gather_fits ? 2 : 0;
+  const int64_t nnz = pr.Ap[pr.n];
+  if (fits && nnz <= kOneCtaMaxNnz) return 1;
+  if (fits && gather_fits && nnz <= kClusterMaxNnz) return 2;
+  return 0;
 }
 
 }  // namespace
@@ -134,11 +151,12 @@ Sol *pdos_ex(const Data *d, const Cone *k, const pdosgpu_options *opt, pdosgpu_i
   Wide w;
   pdosgpu_problem pr;
   if (!to_problem(d, k, w, pr)) return NULL;
-  if (opt && (opt->engine < PDOSGPU_ENGINE_AUTO || opt->engine > PDOSGPU_ENGINE_CTA)) {
+  if (opt && (opt->engine < PDOSGPU_ENGINE_AUTO || opt->engine > PDOSGPU_ENGINE_CLUSTER)) {
     pdosgpu::fail(PDOSGPU_EINVAL, "unknown engine");
     return NULL;
   }
-  if (use_one_cta(pr, opt)) return solve_one_cta(d, pr, opt, info);
+  const int engine = pick_engine(pr, opt);
+  if (engine > 0) return solve_one_cta(d, pr, opt, info, engine == 2);
   pdosgpu_work *work = NULL;
   if (pdosgpu_setup(&pr, opt, &work) != PDOSGPU_OK) return NULL;
   Sol *sol = NULL;

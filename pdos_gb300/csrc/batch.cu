@@ -2083,6 +2083,7 @@ int BatchEngine<T>::append(const pdosgpu_problem *probs, int64_t cnt) {
     return fail(PDOSGPU_EINVAL, "batch_long_row must be 0 or a multiple of 4 in [4, 1024]");
   if (opt_.batch_piece != 0 && (opt_.batch_piece % 4 || opt_.batch_piece < 64 || opt_.batch_piece > 16384))
     return fail(PDOSGPU_EINVAL, "batch_piece must be 0 or a multiple of 4 in [64, 16384]");
+  if (opt_.batch_clusters != 0 && opt_.batch_clusters != 1) return fail(PDOSGPU_EINVAL, "batch_clusters must be 0 or 1");
   PDOS_CUDA_TRY(cudaSetDevice(opt_.device));
   size_t free_b = 0, total_b = 0;
   PDOS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -2410,6 +2411,9 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
     Inst &I = inst_h_[first + i];
     const Smem own{r4(std::max(I.m, I.n)), r4(I.m), r4(I.n), r4(2 * std::max(I.A.npieces, I.At.npieces)), 0, 0, 0};
     if (own.need(sizeof(T)) > (size_t)kSmemLimit) I.cls = kGlobalClass;
+    // on request every instance whose gather vector fits shared memory runs
+    // on a cluster (the global class gathering from shared memory)
+    if (opt_.batch_clusters && (size_t)r4(std::max(I.m, I.n)) * sizeof(T) <= (size_t)kSmemLimit) I.cls = kGlobalClass;
   }
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // the wave's set-up arrays are released next
   layout_arenas_.push_back(std::move(arena));

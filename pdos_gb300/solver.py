@@ -21,11 +21,12 @@ _PRECISION = {"fp64": _lib.PDOSGPU_FP64, "fp32": _lib.PDOSGPU_FP32}
 _SCALING = {"2norm": _lib.PDOSGPU_SCALE_2NORM, "ruiz": _lib.PDOSGPU_SCALE_RUIZ}
 
 
-_ENGINE = {"auto": _lib.PDOSGPU_ENGINE_AUTO, "grid": _lib.PDOSGPU_ENGINE_GRID, "cta": _lib.PDOSGPU_ENGINE_CTA}
+_ENGINE = {"auto": _lib.PDOSGPU_ENGINE_AUTO, "grid": _lib.PDOSGPU_ENGINE_GRID, "cta": _lib.PDOSGPU_ENGINE_CTA,
+           "cluster": _lib.PDOSGPU_ENGINE_CLUSTER}
 
 
 def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True, engine="auto",
-                 layout=None):
+                 layout=None, clusters=False):
     """Options of the C ABI; layout = (long_row, piece) of batch layouts, None for the defaults."""
     if precision not in _PRECISION:
         raise ValueError(f"precision must be one of {sorted(_PRECISION)}")
@@ -42,6 +43,7 @@ def make_options(precision="fp64", scaling="2norm", device=0, share_layouts=True
     opt.engine = _ENGINE[engine]
     if layout is not None:
         opt.batch_long_row, opt.batch_piece = int(layout[0]), int(layout[1])
+    opt.batch_clusters = 1 if clusters else 0
     return opt
 
 
@@ -185,14 +187,15 @@ class Batch:
     """Many independent problems solved together (pdosgpu_batch_*): one CTA
     per instance at a time, convergence masking, per-instance results."""
 
-    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0, share_layouts=True, layout=None):
+    def __init__(self, probs, precision="fp64", device=0, iters_per_launch=0, share_layouts=True, layout=None,
+                 clusters=False):
         self.lib = _lib.load()
         probs = list(probs)
         self.probs = probs
         self.sizes = [(p.n, p.m) for p in probs]
         keep = []
         arr = _c_problems(probs, keep)
-        self._opt = make_options(precision, "2norm", device, share_layouts, layout=layout)
+        self._opt = make_options(precision, "2norm", device, share_layouts, layout=layout, clusters=clusters)
         self._b = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_batch_setup(arr, len(probs), ctypes.byref(self._opt),
                                                 int(iters_per_launch), ctypes.byref(self._b)),
