@@ -1009,10 +1009,10 @@ def main():
         wl = BATCH_WORKLOADS[args.workload]
         if args.impl == "reference":
             return run_batch_reference(args, wl)
+        if args.profile_iters:  # a small batch of the workload's instances (all on the host at once)
+            return profile_batch(args, wl)
         if wl["kind"] == "mix_waves":
             return run_batch_waves(args, wl)
-        if args.profile_iters:
-            return profile_batch(args, wl)
         return run_batch(args, wl)
     wl = WORKLOADS[args.workload]
     prob = make_problem(wl)
