@@ -90,13 +90,20 @@ void set_status(Sol *sol, int solved) {
 }
 
 // Nonzeros up to which pdos() solves a problem with one CTA of the batch
-// kernel: every ADMM iteration then runs inside one launch with CTA
-// barriers only, where the grid engine launches 2k + 4 kernels per
-// iteration (k CG steps) and waits on each.  Measured in FP64 on GB300
-// (solve time, set-up excluded): 2.7x faster on a 1,308-nonzero fixture,
-// 2.4x at 2,761 nonzeros, 1.3x at 23,201; at 86,401 the grid engine is
-// 2.3x faster, since one SM issues only about two FP64 FMAs per clock.
-constexpr int64_t kOneCtaMaxNnz = 32768;
+// kernel, and above that up to which with one 8-CTA cluster: every ADMM
+// iteration then runs inside one launch, where the grid engine launches
+// 2k + 4 kernels per iteration (k CG steps) and waits on each.  Measured in
+// FP64 on GB300 (solve time, set-up excluded), grid / one CTA / cluster:
+// 1,308 nonzeros 7.9 / 2.8 / 3.0 ms; 2,761: 302 / 124 / 126 ms; 23,201:
+// 307 / 190 / 88 ms; 86,401: 218 / 523 / 158 ms; 332,801: 360 / 1,925 /
+// 391 ms.  One SM issues only about two FP64 FMAs per clock, so a single CTA
+// falls behind early; a cluster has eight SMs.
+constexpr int64_t kOneCtaMaxNnz = 4096;
+// Nonzeros up to which pdos() solves on one 8-CTA cluster (above
+// kOneCtaMaxNnz); its gather vector must fit one CTA's shared memory.
+constexpr int64_t kClusterMaxNnz = 200000;
+// CTA size of that cluster: 256 threads below this many nonzeros, else 512.
+constexpr int64_t kClusterSmallNnz = 131072;
 
 // pdos() through the one-CTA path: a batch of one instance, run to its stop
 // test in one launch of the persistent kernel (CTA size by size class).
@@ -110,7 +117,12 @@ Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_optio
   if (pdosgpu_batch_setup(&pr, 1, &o, 0, &b) != PDOSGPU_OK) return NULL;
   Sol *sol = NULL;
   pdosgpu_info inf;
-  if (pdosgpu_batch_solve(b) == PDOSGPU_OK) {
+  int rc = PDOSGPU_OK;
+  if (cluster && pr.Ap[pr.n] < kClusterSmallNnz) {
+    const int blocks[5] = {256, 256, 256, 256, 256};
+    rc = pdosgpu_batch_set_blocks(b, blocks);
+  }
+  if (rc == PDOSGPU_OK && pdosgpu_batch_solve(b) == PDOSGPU_OK) {
     sol = new_sol(d->n, d->m);
     if (sol && pdosgpu_batch_fetch(b, 0, 1, sol->x, sol->s, sol->y, &inf) != PDOSGPU_OK) {
       freeSol(&sol);
@@ -123,9 +135,6 @@ Sol *solve_one_cta(const Data *d, const pdosgpu_problem &pr, const pdosgpu_optio
   return sol;
 }
 
-// Nonzeros up to which pdos() solves on one 8-CTA cluster (above
-// kOneCtaMaxNnz); its gather vector must fit one CTA's shared memory.
-constexpr int64_t kClusterMaxNnz = 0;
 
 // 0: grid engine, 1: one CTA, 2: one cluster.
 int pick_engine(const pdosgpu_problem &pr, const pdosgpu_options *opt) {

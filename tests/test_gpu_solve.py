@@ -31,17 +31,18 @@ def test_workspace_fp64_matches_reference(built_lib, gpu, name):
     check_parity(prob, ref, out, vec_tol=1e-4 if long_run else VEC_TOL)
 
 
+@pytest.mark.parametrize("engine", ["cta", "cluster"])
 @pytest.mark.parametrize("name", solve_cases())
-def test_pdos_one_cta_path_matches_reference(built_lib, gpu, name):
-    """pdos_ex on the one-CTA path (the whole ADMM loop in one launch of the
-    batch kernel, the default for small problems) at the same bar as the
-    grid engine; Ruiz equilibration and the VERBOSE table stay on the grid
-    engine."""
+def test_pdos_one_launch_paths_match_reference(built_lib, gpu, name, engine):
+    """pdos_ex on the one-launch paths -- one CTA, or one 8-CTA cluster, runs
+    the whole ADMM loop in one launch of the batch kernel (the defaults for
+    small and mid-sized problems) -- at the same bar as the grid engine;
+    Ruiz equilibration and the VERBOSE table stay on the grid engine."""
     from pdos_gb300.solver import pdos_call
     prob, ref = load_case(name)
     if ref["variant"] == "ruiz":
         pytest.skip("Ruiz equilibration runs on the grid engine")
-    out = pdos_call(prob.with_params(VERBOSE=0), engine="cta")
+    out = pdos_call(prob.with_params(VERBOSE=0), engine=engine)
     long_run = ref["iters"] >= 1000
     check_parity(prob, ref, out, vec_tol=1e-4 if long_run else VEC_TOL)
     assert out["info"]["kernel_launches"] <= 3  # one graph: queue reset and one persistent launch
