@@ -881,20 +881,54 @@ def run_batch(args, wl):
     if rank == 0 and not args.no_spmv:
         spmv = single_instance_spmv(local)
 
-    # ---- plain single-instance GPU ADMM on a few of the same instances
+    # ---- plain single-instance GPU ADMM on a few of the same instances,
+    # cold start, problem resident: the engine pdos() picks for one instance
+    # of this size (one 8-CTA cluster running the whole ADMM loop in one
+    # launch), and the grid engine beside it
     plain_n = min(args.plain, B)
-    plain_s, plain_iters = 0.0, []
+    plain_s, plain_iters, grid_s = 0.0, [], 0.0
     for p in probs[:plain_n]:
+        with Batch([p], precision=prec, device=local, clusters=True) as b1:
+            b1.set_blocks([256] * 5)
+            b1.solve()  # warm-up
+            b1.reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b1.solve()
+            torch.cuda.synchronize()
+            plain_s += time.perf_counter() - t0
+            plain_iters.append(b1.infos()[0]["admm_iters"])
         with Workspace(p, prec, device=local) as w1:
             w1.solve()  # warm-up
             w1.reset()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            r = w1.solve().fetch()
+            w1.solve().fetch()
             torch.cuda.synchronize()
-            plain_s += time.perf_counter() - t0
-            plain_iters.append(r["iters"])
+            grid_s += time.perf_counter() - t0
     plain = plain_n / plain_s if plain_s > 0 else None
+    plain_grid = plain_n / grid_s if grid_s > 0 else None
+
+    # ---- pdos() latency through the C ABI (set-up, solve, fetch) beside the
+    # oracle on one core, on the small portfolio (n = 100) and one instance of
+    # the family
+    latency = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        from pdos_gb300.generators import portfolio
+        from pdos_gb300.solver import pdos_call
+        latency = {}
+        small = portfolio(100, 10, 0.5, seed=0, params=dict(wl["params"], EPS_ABS=5e-3))
+        for name, pr in (("portfolio_n100_eps5e-3", small), ("family_instance", probs[0])):
+            pdos_call(pr, prec, device=local)  # warm-up
+            t0 = time.perf_counter()
+            out = pdos_call(pr, prec, device=local)
+            t_gpu = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            O.port_solve(pr)
+            t_cpu = time.perf_counter() - t0
+            latency[name] = {"pdos_seconds": t_gpu, "oracle_1_core_seconds": t_cpu, "admm_iterations": out["iters"],
+                             "nnz": pr.nnz, "precision": prec}
 
     # ---- end to end through the public API with host buffers
     e2e = None
@@ -954,7 +988,10 @@ def run_batch(args, wl):
             "dtype": "f32 (f64 reductions)" if sv == 4 else "f64", "data": "synthetic (seeded)",
             "config": cfg,
             "plain_gpu_admm": {"value": plain, "unit": "solves/s", "instances": plain_n,
+                               "engine": "one instance on an 8-CTA cluster (what pdos() picks at this size)",
+                               "grid_engine_value": plain_grid,
                                "admm_iterations_mean": float(np.mean(plain_iters)) if plain_iters else None},
+            "pdos_latency": latency,
             "batched_cold": {"value": ws_n * B / (cold_ms / 1e3), "unit": "solves/s",
                              "admm_iterations_mean": float(np.mean(cold_iters)),
                              "admm_iterations_max": int(max(cold_iters))},
