@@ -865,21 +865,22 @@ struct Slot {
   T lam, alpha, oma;
 };
 
+// sl: the two slots' pointers in shared memory (read where used, so they
+// need no registers across the loops).
 template <typename T, int BLOCK>
 __device__ void solve_pair(const Dev<T> &B, const Inst *I2, State *gst0, State *gst1, int iter_cap, P2<T> *g1,
-                           P2<T> *g2, P2<T> *tt, P2<T> *pbuf, double *scratch) {
+                           P2<T> *g2, P2<T> *tt, P2<T> *pbuf, double *scratch, Slot<T> *sl) {
   const int tid = threadIdx.x;
   const Inst &I = I2[0];  // layout, sizes and cones of both
   const int m = I.m, n = I.n, f = I.f, l = I.l;
   const bool two = gst1 != nullptr;
-  Slot<T> sl[2];
-#pragma unroll
-  for (int g = 0; g < 2; ++g) {
-    const Inst &J = I2[g];
-    sl[g] = Slot<T>{B.x + J.col0, B.q + J.col0, B.s + J.row0, B.y + J.row0, B.st + J.row0, B.u + J.row0,
-                    B.ax + J.row0, B.b + J.row0, B.c + J.col0, B.D + J.row0, B.E + J.col0, (T)J.lambda,
-                    (T)J.alpha, (T)(1.0 - J.alpha)};
+  if (tid < 2) {
+    const Inst &J = I2[tid];
+    sl[tid] = Slot<T>{B.x + J.col0, B.q + J.col0, B.s + J.row0, B.y + J.row0, B.st + J.row0, B.u + J.row0,
+                      B.ax + J.row0, B.b + J.row0, B.c + J.col0, B.D + J.row0, B.E + J.col0, (T)J.lambda,
+                      (T)J.alpha, (T)(1.0 - J.alpha)};
   }
+  __syncthreads();
   const T *pvA0 = static_cast<const T *>(I2[0].pvA), *pvA1 = static_cast<const T *>(I2[1].pvA);
   const T *pvT0 = static_cast<const T *>(I2[0].pvT), *pvT1 = static_cast<const T *>(I2[1].pvT);
   State S[2] = {*gst0, two ? *gst1 : *gst0};
@@ -1170,6 +1171,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_kernel(Dev<T> 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double scratch[2 * 6 * (BLOCK / 32)];
   __shared__ Inst s_inst[2];
+  __shared__ Slot<T> s_slot[2];
   __shared__ int s_k;
   P2<T> *g1 = reinterpret_cast<P2<T> *>(smem_raw);
   P2<T> *g2 = g1 + sm.g1;
@@ -1191,7 +1193,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_kernel(Dev<T> 
     }
     __syncthreads();
     solve_pair<T, BLOCK>(B, s_inst, B.state + id0, id1 >= 0 ? B.state + id1 : nullptr, iter_cap, g1, g2, tt, pbuf,
-                         scratch);
+                         scratch, s_slot);
   }
 }
 
