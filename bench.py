@@ -171,11 +171,11 @@ def committed_traffic(workload, kernel):
     return d.get(workload, {}).get(kernel)
 
 
-def batch_traffic(workload, algorithmic_bytes):
+def batch_traffic(workload, algorithmic_bytes, kernel="batch_admm_kernel"):
     """DRAM bytes of the batch kernel over a solve: the committed ncu ratio of
     DRAM bytes to algorithmic bytes (a smaller launch of the same kernel)
     times this solve's algorithmic bytes, or None."""
-    d = committed_traffic(workload, "batch_admm_kernel")
+    d = committed_traffic(workload, kernel)
     if not isinstance(d, dict) or "dram_bytes_per_algorithmic_byte" not in d:
         return None
     return d["dram_bytes_per_algorithmic_byte"] * algorithmic_bytes
@@ -610,9 +610,11 @@ def run_batch_waves(args, wl):
     peak, peak_kind = measured_peaks()
     pm, pb = batch.time_products(1)
     achieved = roof_bytes / (solve_ms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "batch_admm_kernel (whole fused ADMM iteration per CTA)",
+    roofline = {"bound": "hbm", "kernel": "batch_admm_kernel / batch_cluster_kernel (whole fused ADMM "
+                                          "iteration per CTA; instances too large for one CTA's shared "
+                                          "memory on an 8-CTA cluster)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_kind": peak_kind, "traffic": batch_traffic("portfolio_family_warmstart", roof_bytes),
+                "peak_kind": peak_kind, "traffic": batch_traffic(args.workload, roof_bytes, "batch_cluster_kernel"),
                 "algorithmic_bytes_of_solve": roof_bytes, "ms_of_solve": solve_ms,
                 "spmv_products": {"kernel": "batch_products_kernel (u = A p, t = p + A'u)",
                                   "achieved": pb / (pm / 1e3) / 1e9, "ms": pm, "bytes": pb,
@@ -842,7 +844,9 @@ def run_batch(args, wl):
     peak, peak_kind = measured_peaks()
     achieved = roof_bytes / (cold_ms / 1e3) / 1e9
     pm, pb = batch.time_products(4)
-    roofline = {"bound": "hbm", "kernel": "batch_admm_kernel (whole fused ADMM iteration per CTA)",
+    roofline = {"bound": "hbm", "kernel": "batch_pair_kernel / batch_admm_kernel (whole fused ADMM "
+                                          "iteration per CTA; family instances two per CTA where their "
+                                          "vectors fit twice in shared memory)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind,
                 "traffic": batch_traffic(args.workload, roof_bytes),
