@@ -885,6 +885,33 @@ def run_batch(args, wl):
     if rank == 0 and not args.no_spmv:
         spmv = single_instance_spmv(local)
 
+    # ---- the same instances in the reference's arithmetic: an FP64 batch
+    # (FP64 storage, products and reductions) from the cold start, its CG
+    # products alone beside it, its results against the FP64 oracle
+    batched_fp64 = None
+    if not args.no_fp64 and sv == 4:
+        with Batch(probs, precision="fp64", device=local, share_layouts=not args.own_layouts) as b64:
+            blocks64 = b64.tune(2)
+            b64.reset()
+            s64 = torch.cuda.ExternalStream(b64.stream)
+            barrier()
+            ev0.record(s64)
+            b64.solve()
+            ev1.record(s64)
+            ev1.synchronize()
+            ms64 = ev0.elapsed_time(ev1)
+            inf64 = b64.infos()
+            pm64, pb64 = b64.time_products(2)
+            batched_fp64 = {
+                "value": ws_n * B / (ms64 / 1e3), "unit": "solves/s", "precision": "fp64",
+                "cta_sizes_by_class": blocks64,
+                "admm_iterations_mean": float(np.mean([d["admm_iters"] for d in inf64])),
+                "solved": int(sum(d["solved"] for d in inf64)),
+                "spmv_products": {"achieved": pb64 / (pm64 / 1e3) / 1e9, "unit": "GB/s", "ms": pm64,
+                                  "bytes": pb64},
+                "objective_error_vs_fp64_oracle": check.summary(probs, b64.fetch_all()[0])
+                if check is not None else None}
+
     # ---- plain single-instance GPU ADMM on a few of the same instances,
     # cold start, problem resident: the engine pdos() picks for one instance
     # of this size (one 8-CTA cluster running the whole ADMM loop in one
@@ -932,6 +959,7 @@ def run_batch(args, wl):
             O.port_solve(pr)
             t_cpu = time.perf_counter() - t0
             latency[name] = {"pdos_seconds": t_gpu, "oracle_1_core_seconds": t_cpu, "admm_iterations": out["iters"],
+                             "setup_ms": out["info"]["setup_ms"], "solve_ms": out["info"]["solve_ms"],
                              "nnz": pr.nnz, "precision": prec}
 
     # ---- end to end through the public API with host buffers
@@ -999,6 +1027,7 @@ def run_batch(args, wl):
             "batched_cold": {"value": ws_n * B / (cold_ms / 1e3), "unit": "solves/s",
                              "admm_iterations_mean": float(np.mean(cold_iters)),
                              "admm_iterations_max": int(max(cold_iters))},
+            "batched_cold_fp64": batched_fp64,
             "speedup_vs_plain_gpu_admm": (value / plain) if plain else None,
             "admm_iterations_mean": float(np.mean(warm_iters)),
             "admm_iterations_max": int(max(warm_iters)),
@@ -1042,6 +1071,8 @@ def main():
                     help="batch workloads: every instance keeps its own matrix layout (no family sharing)")
     ap.add_argument("--no-spmv", action="store_true",
                     help="skip the single-instance SpMV block of the batch workloads")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the FP64 batch of the family workload")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling case: set up the workload, run this many ADMM "
                          "iterations, print nothing else (for ncu)")
