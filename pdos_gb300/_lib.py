@@ -136,7 +136,7 @@ _libs = {}
 def lib_file(name="libpdosindir.so"):
     """Path of an in-tree library; PDOS_GB300_LIB_DIR points elsewhere (for
     side-by-side builds of different kernel configurations)."""
-    return os.path.join(os.environ.get("PDOS_GB300_LIB_DIR", LIB_DIR), name)
+    return os.path.join(os.environ.get("PDOS_GB300_LIB_DIR") or LIB_DIR, name)
 
 
 def load(name="libpdosindir.so"):

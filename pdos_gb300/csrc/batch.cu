@@ -1643,7 +1643,7 @@ __global__ void warm_start_kernel(const double *x0, const double *y0, const doub
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n + m;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (i < n) {
-      if (x0) xi[i] = (T)((x0[i] / Epre[i]) / 1e3);
+      if (x0) xi[i] = (T)((x0[i] / Epre[i]) / kXRatio);
     } else {
       const int64_t r = i - n;
       if (y0) yi[r] = (T)(y0[r] / D[r]);
@@ -1662,15 +1662,6 @@ __global__ void gather_values_kernel(const int32_t *src, int64_t count, const T 
     const int32_t p = src[i];
     to[i] = p >= 0 ? from[p] : (p == -1 ? T(0) : nan_box(T(0), (uint32_t)(-2 - p)));
   }
-}
-
-// Values at 64-bit source positions (the varying entries of a family group's
-// instances in the wave's stacked arrays).
-template <typename T>
-__global__ void gather_values64_kernel(const int64_t *src, int64_t count, const T *from, T *to) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
-       i += (int64_t)gridDim.x * blockDim.x)
-    to[i] = from[src[i]];
 }
 
 // ------------------------------------------------------------ host side
@@ -2115,7 +2106,22 @@ int BatchEngine<T>::append(const pdosgpu_problem *probs, int64_t cnt) {
 // the wave's vectors until commit().
 template <typename T>
 int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
-  int64_t N = 0, M = 0, NNZ = 0;
+  // ---- family groups share one layout (NORMALIZE = 0 only: scaling would
+  // give every instance its own values).  With NORMALIZE = 0 nothing of the
+  // device set-up but the layout depends on the matrix, so a group's members
+  // after the first enter the stacked problem without their entries: their
+  // varying values are taken from the host arrays below.
+  std::vector<FamilyGroup> groups;
+  std::vector<int32_t> group_of(cnt, -1);
+  std::vector<uint8_t> no_entries(cnt, 0);
+  if (!normalize_ && opt_.batch_layouts == PDOSGPU_BATCH_SHARE) groups = find_family_groups(probs, cnt);
+  for (size_t g = 0; g < groups.size(); ++g) {
+    for (int64_t i : groups[g].members) group_of[i] = (int32_t)g;
+    for (size_t k = 1; k < groups[g].members.size(); ++k) no_entries[groups[g].members[k]] = 1;
+  }
+  auto stacked_nnz = [&](int64_t i) -> int64_t { return no_entries[i] ? 0 : probs[i].Ap[probs[i].n]; };
+
+  int64_t N = 0, M = 0, NNZ = 0, wave_nnz = 0;
   bool any_x = false, any_y = false, any_s = false;
   std::vector<int64_t> wrow0, wcol0;  // offsets inside the wave
   for (int64_t i = 0; i < cnt; ++i) {
@@ -2124,7 +2130,8 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
     wcol0.push_back(N);
     N += p.n;
     M += p.m;
-    NNZ += p.Ap[p.n];
+    NNZ += stacked_nnz(i);
+    wave_nnz += p.Ap[p.n];
     any_x |= p.x0 != nullptr;
     any_y |= p.y0 != nullptr;
     any_s |= p.s0 != nullptr;
@@ -2151,7 +2158,7 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
     std::vector<int64_t> e0(cnt + 1, 0);  // first nonzero of each instance
     for (int64_t i = 0; i < cnt; ++i) {
       const pdosgpu_problem &p = probs[i];
-      e0[i + 1] = e0[i] + p.Ap[p.n];
+      e0[i + 1] = e0[i] + stacked_nnz(i);
       int64_t off = wrow0[i] + p.f + p.l;
       for (int64_t k = 0; k < p.qsize; ++k) {
         d.soc_off.push_back(off);
@@ -2161,8 +2168,8 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
     }
     parallel_for(cnt, [&](int64_t i) {
       const pdosgpu_problem &p = probs[i];
-      const int64_t nz = p.Ap[p.n], e = e0[i];
-      for (int64_t j = 0; j < p.n; ++j) Ap[wcol0[i] + j] = e + p.Ap[j];
+      const int64_t nz = stacked_nnz(i), e = e0[i];
+      for (int64_t j = 0; j < p.n; ++j) Ap[wcol0[i] + j] = nz > 0 ? e + p.Ap[j] : e;
       if (nz > 0) std::memcpy(&Ax[e], p.Ax, sizeof(double) * nz);
       for (int64_t k = 0; k < nz; ++k) Ai[e + k] = wrow0[i] + p.Ai[k];
       std::memcpy(&b[wrow0[i]], p.b, sizeof(double) * p.m);
@@ -2263,13 +2270,6 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
   const int32_t *rp = P.rp_host.data(), *ap = P.ap_host.data();
   const int32_t *rj = Rj.data();
   const int64_t *ai = Ai.data();
-  // ---- family groups share one layout (NORMALIZE = 0 only: scaling would
-  // give every instance its own values)
-  std::vector<FamilyGroup> groups;
-  std::vector<int32_t> group_of(cnt, -1);
-  if (!normalize_ && opt_.batch_layouts == PDOSGPU_BATCH_SHARE) groups = find_family_groups(probs, cnt);
-  for (size_t g = 0; g < groups.size(); ++g)
-    for (int64_t i : groups[g].members) group_of[i] = (int32_t)g;
   {  // instances with their own layout
     std::vector<int64_t> own;
     for (int64_t i = 0; i < cnt; ++i)
@@ -2363,36 +2363,39 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
     HybPtr hA{}, hT{};
     PDOS_TRY(upload_hyb<T>(bA, P.Rx, *arena, st, hA, &layout_bytes));
     PDOS_TRY(upload_hyb<T>(bT, P.Ax, *arena, st, hT, &layout_bytes));
-    // every member's values of the varying entries, in layout order
+    // every member's values of the varying entries, in layout order, from
+    // the host arrays: the same operations as the device set-up with
+    // NORMALIZE = 0 (the x-space ratio, then the conversion to T), after the
+    // finiteness check the device set-up makes of every entry
     const int64_t nm = (int64_t)fg.members.size(), na = (int64_t)vposA.size(), nt = (int64_t)vposT.size();
     T *pvA = nullptr, *pvT = nullptr;
     PDOS_TRY(arena->alloc(&pvA, (size_t)(nm * na)));
     PDOS_TRY(arena->alloc(&pvT, (size_t)(nm * nt)));
     layout_bytes += (nm * na + nm * nt) * (int64_t)sizeof(T);
     {
-      std::vector<int64_t> srcA((size_t)(nm * na)), srcT((size_t)(nm * nt));
-      for (int64_t k = 0; k < nm; ++k) {
-        const int64_t i = fg.members[k];
-        const int64_t rb = rp[wrow0[i]], cb = Ap[wcol0[i]];
-        for (int64_t t = 0; t < na; ++t) srcA[k * na + t] = rb + vposA[t];
-        for (int64_t t = 0; t < nt; ++t) srcT[k * nt + t] = cb + vposT[t];
-      }
-      DeviceArena tmp;
-      int64_t *dA = nullptr, *dT = nullptr;
-      PDOS_TRY(tmp.alloc(&dA, srcA.size()));
-      PDOS_TRY(tmp.alloc(&dT, srcT.size()));
-      if (!srcA.empty()) {
-        PDOS_CUDA_TRY(cudaMemcpyAsync(dA, srcA.data(), sizeof(int64_t) * srcA.size(), cudaMemcpyHostToDevice, st));
-        const int g = (int)std::min<int64_t>(((int64_t)srcA.size() + 255) / 256, (int64_t)num_sms() * 16);
-        gather_values64_kernel<T><<<g, 256, 0, st>>>(dA, (int64_t)srcA.size(), P.Rx, pvA);
-      }
-      if (!srcT.empty()) {
-        PDOS_CUDA_TRY(cudaMemcpyAsync(dT, srcT.data(), sizeof(int64_t) * srcT.size(), cudaMemcpyHostToDevice, st));
-        const int g = (int)std::min<int64_t>(((int64_t)srcT.size() + 255) / 256, (int64_t)num_sms() * 16);
-        gather_values64_kernel<T><<<g, 256, 0, st>>>(dT, (int64_t)srcT.size(), P.Ax, pvT);
-      }
-      PDOS_CUDA_TRY(cudaGetLastError());
-      PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before the host and temporary arrays go
+      Raw<T> hvA, hvT;
+      hvA.resize((size_t)(nm * na));
+      hvT.resize((size_t)(nm * nt));
+      std::atomic<int> bad{0};
+      parallel_for(nm, [&](int64_t k) {
+        const double *ax = probs[fg.members[k]].Ax;
+        for (int64_t t = 0; t < na; ++t) {
+          const double v = ax[csr2csc[vposA[t]]];
+          if (!std::isfinite(v)) bad = 1;
+          hvA[k * na + t] = (T)(v * kXRatio);
+        }
+        for (int64_t t = 0; t < nt; ++t) {
+          const double v = ax[vposT[t]];
+          if (!std::isfinite(v)) bad = 1;
+          hvT[k * nt + t] = (T)(v * kXRatio);
+        }
+      });
+      if (bad) return fail(PDOSGPU_EINVAL, "A, b or c holds NaN or Inf");
+      if (nm * na > 0)
+        PDOS_CUDA_TRY(cudaMemcpyAsync(pvA, hvA.data(), sizeof(T) * nm * na, cudaMemcpyHostToDevice, st));
+      if (nm * nt > 0)
+        PDOS_CUDA_TRY(cudaMemcpyAsync(pvT, hvT.data(), sizeof(T) * nm * nt, cudaMemcpyHostToDevice, st));
+      PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before the host arrays go
     }
     for (int64_t k = 0; k < nm; ++k) {
       Inst &I = inst_h_[first + fg.members[k]];
@@ -2423,7 +2426,7 @@ int BatchEngine<T>::append_wave(const pdosgpu_problem *probs, int64_t cnt) {
   count += cnt;
   total_n += N;
   total_m += M;
-  total_nnz += NNZ;
+  total_nnz += wave_nnz;
   ++waves;
   return PDOSGPU_OK;
 }

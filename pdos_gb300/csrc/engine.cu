@@ -431,10 +431,10 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
   }
   PDOS_TRY(arena.alloc(&P.Epre64, (size_t)n));
   PDOS_CUDA_TRY(cudaMemcpyAsync(P.Epre64, E64, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-  scal_kernel<<<grid1d(n), 256, 0, st>>>(E64, n, 1e3, 0);
-  scal_kernel<<<grid1d(n), 256, 0, st>>>(cw, n, 1e3, 0);
-  scal_kernel<<<grid1d(n), 256, 0, st>>>(xw, n, 1e3, 1);
-  if (nnz > 0) scal_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, nnz, 1e3, 0);
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(E64, n, kXRatio, 0);
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(cw, n, kXRatio, 0);
+  scal_kernel<<<grid1d(n), 256, 0, st>>>(xw, n, kXRatio, 1);
+  if (nnz > 0) scal_kernel<<<grid1d(nnz), 256, 0, st>>>(Aw, nnz, kXRatio, 0);
   PDOS_CUDA_TRY(cudaGetLastError());
 
   // ---- working arrays in T

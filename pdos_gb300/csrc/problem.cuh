@@ -16,6 +16,10 @@
 
 namespace pdosgpu {
 
+// The x-space ratio applied after equilibration (common.h:185-192): E, c and
+// the matrix values are multiplied by it, a warm-start x is divided by it.
+constexpr double kXRatio = 1e3;
+
 struct ProblemDesc {
   int64_t n = 0, m = 0, nnz = 0;
   const double *Ax = nullptr;
