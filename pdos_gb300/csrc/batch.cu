@@ -1252,7 +1252,10 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_products_kerne
 // memory through distributed shared memory, in rank order, so every thread
 // of the cluster holds the same totals.  Per-row sums are those of the
 // one-CTA kernel; only the order of the block sums differs.
-constexpr int kClusterCtas = 8;  // portable cluster size
+#ifndef PDOS_BATCH_CLUSTER
+#define PDOS_BATCH_CLUSTER 8
+#endif
+constexpr int kClusterCtas = PDOS_BATCH_CLUSTER;  // CTAs per cluster (portable sizes: at most 8)
 
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
@@ -1851,8 +1854,8 @@ struct FamilyGroup {
   int64_t nvary = 0;
 };
 
-// 64-bit mix of the words of a problem's pattern (a filter; equality is
-// checked exactly afterwards).
+// 64-bit mix of a problem's shape, cones and a sample of its pattern (a
+// filter: equality is checked exactly afterwards).
 inline uint64_t pattern_hash(const pdosgpu_problem &p) {
   uint64_t h = 0x9E3779B97F4A7C15ull;
   auto mix = [&](uint64_t v) {
@@ -1865,9 +1868,12 @@ inline uint64_t pattern_hash(const pdosgpu_problem &p) {
   mix((uint64_t)p.l);
   mix((uint64_t)p.qsize);
   for (int64_t k = 0; k < p.qsize; ++k) mix((uint64_t)p.q[k]);
-  for (int64_t j = 0; j <= p.n; ++j) mix((uint64_t)p.Ap[j]);
+  constexpr int64_t kStride = 61;  // every 61st entry of Ap and Ai, and the last
+  for (int64_t j = 0; j <= p.n; j += kStride) mix((uint64_t)p.Ap[j]);
+  mix((uint64_t)p.Ap[p.n]);
   const int64_t nz = p.Ap[p.n];
-  for (int64_t k = 0; k < nz; ++k) mix((uint64_t)p.Ai[k]);
+  for (int64_t k = 0; k < nz; k += kStride) mix((uint64_t)p.Ai[k]);
+  if (nz > 0) mix((uint64_t)p.Ai[nz - 1]);
   return h;
 }
 

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "batch_layout.h"
 #include "engine.cuh"
 #include "problem.cuh"
 #include "setup_kernels.cuh"
@@ -220,13 +221,13 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
   {  // DIMACS denominators from the caller's b and c (pdos.c:76-77)
     P.pscale.assign(ninst, 1.0);
     P.dscale.assign(ninst, 1.0);
-    for (int64_t k = 0; k < ninst; ++k) {
+    batch::parallel_for(ninst, [&](int64_t k) {  // instances in parallel, each summed in order
       double sb = 0.0, sc = 0.0;
       for (int64_t i = d.inst_row0[k]; i < d.inst_row0[k + 1]; ++i) sb += d.b[i] * d.b[i];
       for (int64_t j = d.inst_col0[k]; j < d.inst_col0[k + 1]; ++j) sc += d.c[j] * d.c[j];
       P.pscale[k] = 1.0 + std::sqrt(sb);
       P.dscale[k] = 1.0 + std::sqrt(sc);
-    }
+    });
   }
 
   DeviceArena tmp;  // set-up temporaries
@@ -301,8 +302,9 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
   int64_t *cone_off = nullptr, *cone_len = nullptr;
   if (ncones > 0) {
     cone_of_row_h.assign(m, -1);
-    for (int64_t c = 0; c < ncones; ++c)
+    batch::parallel_for(ncones, [&](int64_t c) {
       for (int64_t i = 0; i < d.soc_len[c]; ++i) cone_of_row_h[d.soc_off[c] + i] = (int32_t)c;
+    });
     PDOS_TRY(tmp.alloc(&cone_of_row, (size_t)m));
     PDOS_TRY(tmp.alloc(&cone_off, (size_t)ncones));
     PDOS_TRY(tmp.alloc(&cone_len, (size_t)ncones));
@@ -422,12 +424,12 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
     PDOS_CUDA_TRY(cudaStreamSynchronize(st));
     const double guard = ruiz ? 1e-6 : 1e-15;
     P.lambda.assign(ninst, 1.0);
-    for (int64_t k = 0; k < ninst; ++k) {
+    batch::parallel_for(ninst, [&](int64_t k) {
       double sb = 0.0, sc = 0.0;
       for (int64_t i = d.inst_row0[k]; i < d.inst_row0[k + 1]; ++i) sb += hb[i] * hb[i];
       for (int64_t j = d.inst_col0[k]; j < d.inst_col0[k + 1]; ++j) sc += hc[j] * hc[j];
       P.lambda[k] = (guard + std::sqrt(sb)) / (guard + std::sqrt(sc));
-    }
+    });
   }
   PDOS_TRY(arena.alloc(&P.Epre64, (size_t)n));
   PDOS_CUDA_TRY(cudaMemcpyAsync(P.Epre64, E64, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -468,7 +470,9 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
   P.ap_host.assign((size_t)n + 1, 0);
   PDOS_CUDA_TRY(cudaMemcpyAsync(P.rp_host.data(), P.Rp, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, st));
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-  for (int64_t j = 0; j <= n; ++j) P.ap_host[j] = (int32_t)d.Ap[j];
+  batch::parallel_for((n + 1 + 65535) / 65536, [&](int64_t c) {
+    for (int64_t j = c * 65536; j < std::min<int64_t>(n + 1, (c + 1) * 65536); ++j) P.ap_host[j] = (int32_t)d.Ap[j];
+  });
   tmp.release();
   return PDOSGPU_OK;
 }
