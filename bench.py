@@ -612,7 +612,7 @@ def run_batch_waves(args, wl):
     achieved = roof_bytes / (solve_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "batch_admm_kernel / batch_cluster_kernel (whole fused ADMM "
                                           "iteration per CTA; instances too large for one CTA's shared "
-                                          "memory on an 8-CTA cluster)",
+                                          "memory on a 4-CTA cluster)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind, "traffic": batch_traffic(args.workload, roof_bytes, "batch_cluster_kernel"),
                 "algorithmic_bytes_of_solve": roof_bytes, "ms_of_solve": solve_ms,
@@ -849,7 +849,8 @@ def run_batch(args, wl):
                                           "vectors fit twice in shared memory)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind,
-                "traffic": batch_traffic(args.workload, roof_bytes),
+                "traffic": batch_traffic(args.workload, roof_bytes, "batch_pair_kernel")
+                or batch_traffic(args.workload, roof_bytes),
                 "algorithmic_bytes_per_solve_of_batch": roof_bytes, "ms_per_solve_of_batch": cold_ms,
                 "spmv_products": {"kernel": "batch_products_kernel (u = A p, t = p + A'u)",
                                   "achieved": pb / (pm / 1e3) / 1e9, "ms": pm, "bytes": pb,

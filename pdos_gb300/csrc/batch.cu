@@ -1243,7 +1243,7 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_products_kerne
 
 // ---------------------------------------------------------------- clusters
 // Large instances of the global-staging class run on a thread-block cluster
-// of kClusterCtas CTAs (one per SM): the warps of the whole cluster share
+// of C CTAs (one per SM): the warps of the whole cluster share
 // each product's pieces and slices, the element-wise loops are spread over
 // the cluster's threads, every CTA copies the vector a product gathers from
 // into its own shared memory, the staged vectors live in one global region
@@ -1252,10 +1252,19 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_products_kerne
 // memory through distributed shared memory, in rank order, so every thread
 // of the cluster holds the same totals.  Per-row sums are those of the
 // one-CTA kernel; only the order of the block sums differs.
-#ifndef PDOS_BATCH_CLUSTER
-#define PDOS_BATCH_CLUSTER 8
-#endif
-constexpr int kClusterCtas = PDOS_BATCH_CLUSTER;  // CTAs per cluster (portable sizes: at most 8)
+// The cluster size is chosen at launch: 4 CTAs for a batch's class (more
+// clusters fit the device at once -- its GPCs hold 16 of their SMs in 8-CTA
+// clusters -- and a cluster synchronises fewer CTAs), 8 for pdos() on one
+// instance, which has the device to itself.
+constexpr int kClusterMax = 8;       // portable cluster size limit
+constexpr int kClusterCtasBatch = 4;
+constexpr int kClusterCtasOne = 8;
+
+__device__ __forceinline__ int cluster_ctas() {
+  uint32_t n;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+  return (int)n;
+}
 
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
@@ -1294,11 +1303,12 @@ struct ClusterBarrier {
 // totals stored into slot r of CTA 0, a cluster barrier, then every warp
 // loads the C slots into its lanes and runs the xor butterfly -- the same
 // bits everywhere.  Two slot halves are used in turn, as in Reduce.
-template <int BLOCK, int C>
+template <int BLOCK>
 struct ClusterReduce {
   double *scratch;  // this CTA: 2 x 3 x BLOCK/32
-  double *slots;    // every CTA's copy; CTA 0's is the one used: 2 x 3 x C
+  double *slots;    // every CTA's copy; CTA 0's is the one used: 2 x 3 x kClusterMax
   uint32_t rank;
+  int C;            // CTAs in the cluster
   int half;
   template <int N>
   __device__ __forceinline__ void operator()(double (&v)[N]) {
@@ -1306,13 +1316,13 @@ struct ClusterReduce {
     block_sum_n<BLOCK, N>(v, scratch + half * 3 * (BLOCK / 32));
     if (threadIdx.x == 0) {
 #pragma unroll
-      for (int k = 0; k < N; ++k) st_dsmem(dsmem_addr(&slots[(half * 3 + k) * C + rank], 0), v[k]);
+      for (int k = 0; k < N; ++k) st_dsmem(dsmem_addr(&slots[(half * 3 + k) * kClusterMax + rank], 0), v[k]);
     }
     cluster_sync();
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < N; ++k)
-      v[k] = warp_sum(lane < C ? ld_dsmem(dsmem_addr(&slots[(half * 3 + k) * C + lane], 0)) : 0.0);
+      v[k] = warp_sum(lane < C ? ld_dsmem(dsmem_addr(&slots[(half * 3 + k) * kClusterMax + lane], 0)) : 0.0);
   }
 };
 
@@ -1320,10 +1330,12 @@ struct ClusterReduce {
 // memory): the operations and their order are those of solve_instance with
 // SG; rows are shared among the cluster's warps and element-wise loops
 // among its threads.
-template <typename T, int BLOCK, int C>
+template <typename T, int BLOCK>
 __device__ void solve_instance_cluster(const Dev<T> &B, const Inst &I, State *gst, int iter_cap, T *g1, T *g2,
-                                       T *tt, T *pbuf, double *scratch, double *slots, T *gs, uint32_t rank) {
-  constexpr int W = BLOCK / 32, CT = C * BLOCK;
+                                       T *tt, T *pbuf, double *scratch, double *slots, T *gs, uint32_t rank,
+                                       int C) {
+  constexpr int W = BLOCK / 32;
+  const int CT = C * BLOCK;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int ct = (int)rank * BLOCK + tid;  // thread index in the cluster
   const Part part{(int)rank * W + warp, C * W, ct, CT};
@@ -1345,7 +1357,7 @@ __device__ void solve_instance_cluster(const Dev<T> &B, const Inst &I, State *gs
 
   State S = *gst;  // the same in every thread of the cluster
   if (S.done) return;
-  ClusterReduce<BLOCK, C> reduce{scratch, slots, rank, 0};
+  ClusterReduce<BLOCK> reduce{scratch, slots, rank, C, 0};
 
   auto finish = [&](int r, T sv, T stv, T axv, double &pr2, double &byv) {
     const T yv = y[r] + (sv - stv) / lam;
@@ -1553,10 +1565,10 @@ __device__ __forceinline__ int cluster_next(int *queue, int *s_k, uint32_t rank)
 
 template <typename T, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 1) batch_cluster_kernel(Dev<T> B, int cls, Smem sm, int iter_cap) {
-  constexpr int C = kClusterCtas;
+  const int C = cluster_ctas();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double scratch[2 * 3 * (BLOCK / 32)];
-  __shared__ double slots[2 * 3 * C];
+  __shared__ double slots[2 * 3 * kClusterMax];
   __shared__ Inst s_inst;
   __shared__ int s_k;
   const uint32_t rank = cluster_rank();
@@ -1573,8 +1585,8 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_cluster_kernel(Dev<T> B, int c
     if (threadIdx.x < (int)(sizeof(Inst) / 4))
       reinterpret_cast<int32_t *>(&s_inst)[threadIdx.x] = reinterpret_cast<const int32_t *>(B.inst + id)[threadIdx.x];
     __syncthreads();
-    solve_instance_cluster<T, BLOCK, C>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch, slots, gs,
-                                        rank);
+    solve_instance_cluster<T, BLOCK>(B, s_inst, B.state + id, iter_cap, g1, g2, tt, pbuf, scratch, slots, gs,
+                                     rank, C);
   }
   cluster_sync();  // no CTA leaves while another may still read its shared memory
 }
@@ -1582,7 +1594,8 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_cluster_kernel(Dev<T> B, int c
 // The two CG products alone on clusters (roofline timing of that class).
 template <typename T, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 1) batch_cluster_products_kernel(Dev<T> B, int cls, Smem sm, int reps) {
-  constexpr int C = kClusterCtas, W = BLOCK / 32;
+  constexpr int W = BLOCK / 32;
+  const int C = cluster_ctas();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Inst s_inst;
   __shared__ int s_k;
@@ -1752,7 +1765,7 @@ inline int stage_mode(const Smem &sm) {
   return !sm.global ? kStageShared : (sm.gs > 0 ? kStageGlobalSG : kStageGlobal);
 }
 // A global-staging class whose gather vectors fit shared memory runs on
-// clusters of kClusterCtas CTAs, one instance per cluster.
+// clusters, one instance per cluster.
 inline bool on_clusters(const Smem &sm) { return stage_mode(sm) == kStageGlobalSG; }
 template <typename T>
 KernelOf<T> cluster_kernel_for(int block, bool products) {
@@ -1765,14 +1778,14 @@ KernelOf<T> cluster_kernel_for(int block, bool products) {
   }
 }
 inline cudaLaunchConfig_t cluster_config(int grid, int block, size_t bytes, cudaStream_t st,
-                                         cudaLaunchAttribute *attr) {
+                                         cudaLaunchAttribute *attr, int ctas) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)block);
   cfg.dynamicSmemBytes = bytes;
   cfg.stream = st;
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kClusterCtas;
+  attr[0].val.clusterDim.x = (unsigned)ctas;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
@@ -1795,24 +1808,24 @@ int allow_dynamic_smem(K kernel, size_t need) {
   return PDOSGPU_OK;
 }
 
-// Grid (a multiple of kClusterCtas) of a cluster kernel: as many clusters as
-// fit the device at once, at most one per instance and per staging region.
+// Grid (a multiple of `ctas`) of a cluster kernel: as many clusters as fit
+// the device at once, at most one per instance and per staging region.
 template <typename T>
-int cluster_grid(KernelOf<T> kernel, int block, size_t bytes, int members, int regions, int *grid) {
+int cluster_grid(KernelOf<T> kernel, int block, size_t bytes, int members, int regions, int ctas, int *grid) {
   PDOS_TRY(allow_dynamic_smem(kernel, bytes));
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = cluster_config(kClusterCtas, block, bytes, nullptr, attr);
+  cudaLaunchConfig_t cfg = cluster_config(ctas, block, bytes, nullptr, attr, ctas);
   int nc = 0;
   PDOS_CUDA_TRY(cudaOccupancyMaxActiveClusters(&nc, (const void *)kernel, &cfg));
   if (nc < 1) return fail(PDOSGPU_ENOTSUP, "a cluster of the batch kernel does not fit the device");
-  *grid = std::max(1, std::min(std::min(members, nc), regions)) * kClusterCtas;
+  *grid = std::max(1, std::min(std::min(members, nc), regions)) * ctas;
   return PDOSGPU_OK;
 }
 template <typename T>
 int launch_clusters(KernelOf<T> kernel, int grid, int block, size_t bytes, cudaStream_t st, const Dev<T> &dev,
-                    int cls, const Smem &sm, int arg) {
+                    int cls, const Smem &sm, int arg, int ctas) {
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = cluster_config(grid, block, bytes, st, attr);
+  cudaLaunchConfig_t cfg = cluster_config(grid, block, bytes, st, attr, ctas);
   PDOS_CUDA_TRY(cudaLaunchKernelEx(&cfg, kernel, dev, cls, sm, arg));
   return PDOSGPU_OK;
 }
@@ -2030,6 +2043,7 @@ class BatchEngine : public BatchBase {
   std::vector<cudaGraphExec_t> exec_;  // [0]: one launch of iter_cap iterations
   int iter_cap_ = 64;
   int gregions_ = 0;  // staging regions allocated for the global class
+  int cluster_ctas_ = kClusterCtasBatch;  // CTAs per cluster of the global class
   Dev<T> dev_{};
   Inst *inst_d_ = nullptr;
   State *state_d_ = nullptr;
@@ -2577,7 +2591,8 @@ int BatchEngine<T>::commit() {
   B.gscratch = nullptr;
   {  // one staging region per resident CTA (at most 8 per SM) or cluster of the global class
     const int members_g = class_begin_h_[kGlobalClass + 1] - class_begin_h_[kGlobalClass];
-    gregions_ = on_clusters(smem_[kGlobalClass]) ? std::min(members_g, std::max(1, num_sms() / kClusterCtas))
+    cluster_ctas_ = opt_.batch_clusters ? kClusterCtasOne : kClusterCtasBatch;
+    gregions_ = on_clusters(smem_[kGlobalClass]) ? std::min(members_g, std::max(1, num_sms() / cluster_ctas_))
                                                  : std::min(members_g, num_sms() * (1024 / kBlocks[0]));
     if (gregions_ > 0) PDOS_TRY(arena_.alloc(&B.gscratch, (size_t)gregions_ * smem_[kGlobalClass].stride()));
   }
@@ -2628,7 +2643,7 @@ int BatchEngine<T>::configure(int cls, int block) {
   if (on_clusters(smem_[cls])) {
     auto kernel = cluster_kernel_for<T>(block, false);
     if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
-    return cluster_grid<T>(kernel, block, bytes, members, gregions_, &grid_[cls]);
+    return cluster_grid<T>(kernel, block, bytes, members, gregions_, cluster_ctas_, &grid_[cls]);
   }
   auto kernel = admm_kernel_for<T>(block, smem_[cls]);
   if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
@@ -2642,7 +2657,7 @@ int BatchEngine<T>::launch_class(int cls, int block, int iter_cap, cudaStream_t 
   if (on_clusters(sm)) {
     auto kernel = cluster_kernel_for<T>(block, false);
     if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
-    return launch_clusters<T>(kernel, grid_[cls], block, bytes, st, dev_, cls, sm, iter_cap);
+    return launch_clusters<T>(kernel, grid_[cls], block, bytes, st, dev_, cls, sm, iter_cap, cluster_ctas_);
   }
   auto kernel = admm_kernel_for<T>(block, sm);
   if (!kernel) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
@@ -2897,8 +2912,9 @@ int BatchEngine<T>::time_products(int reps, double *ms, double *bytes) {
       auto ck = cluster_kernel_for<T>(block, true);
       if (!ck) return fail(PDOSGPU_EINVAL, "unsupported CTA size");
       int grid = 0;
-      PDOS_TRY(cluster_grid<T>(ck, block, sm_bytes, class_begin_h_[cls + 1] - class_begin_h_[cls], gregions_, &grid));
-      return launch_clusters<T>(ck, grid, block, sm_bytes, st, dev_, cls, smem_[cls], reps);
+      PDOS_TRY(cluster_grid<T>(ck, block, sm_bytes, class_begin_h_[cls + 1] - class_begin_h_[cls], gregions_,
+                               cluster_ctas_, &grid));
+      return launch_clusters<T>(ck, grid, block, sm_bytes, st, dev_, cls, smem_[cls], reps, cluster_ctas_);
     }
     PDOS_TRY(allow_dynamic_smem(kernel, sm_bytes));
     int per_sm = 0;
