@@ -60,10 +60,10 @@ typedef struct {
                          [4, 1024]) */
   int batch_piece;    /* batches only: nonzeros per piece at most (0: 1,024;
                          else a multiple of 4 in [64, 16384]) */
-  int batch_clusters; /* batches only: 0 (default) runs on 8-CTA clusters only
+  int batch_clusters; /* batches only: 0 (default) runs on 4-CTA clusters only
                          the instances too large for one CTA's shared memory;
                          1 runs every instance whose gather vector fits
-                         shared memory on a cluster */
+                         shared memory on an 8-CTA cluster */
 } pdosgpu_options;
 
 typedef struct {
