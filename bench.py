@@ -463,6 +463,8 @@ def profile_batch(args, wl):
     fam, mus, ds, probs = batch_instances(wl, args.batch or 64, 0)
     with Batch(probs, precision=wl["precision"], iters_per_launch=args.profile_iters,
                share_layouts=not args.own_layouts) as b:
+        if args.blocks:  # the CTA size of each class, as the tuner would set it
+            b.set_blocks([int(v) for v in args.blocks.split(",")])
         if fam is not None:
             from pdos_gb300.warmstart import FamilyWarmStart
             ws = FamilyWarmStart(fam, hidden=wl["hidden"], max_batch=len(probs), seed=0)
@@ -1072,6 +1074,8 @@ def main():
                     help="batch workloads: every instance keeps its own matrix layout (no family sharing)")
     ap.add_argument("--no-spmv", action="store_true",
                     help="skip the single-instance SpMV block of the batch workloads")
+    ap.add_argument("--blocks", default="",
+                    help="profiling case: CTA size of each of the five size classes, comma-separated")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the FP64 batch of the family workload")
     ap.add_argument("--profile-iters", type=int, default=0,
