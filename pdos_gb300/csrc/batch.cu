@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "batch_layout.h"
+#include "batch_family.h"
 #include "engine.cuh"
 #include "problem.cuh"
 
@@ -209,11 +210,9 @@ __device__ __forceinline__ Val4<double> ld_stream4(const double *p) {
 }
 
 // Varying entries of a shared (family) layout: the shared value array holds
-// a quiet NaN whose low 22 bits index the instance's own value of that
-// entry.  Input data is checked finite at set-up, so no genuine value is a
-// NaN.
-constexpr uint32_t kBoxBits = 22;
-__host__ __device__ __forceinline__ bool box_index_fits(int64_t t) { return t >= 0 && t < ((int64_t)1 << kBoxBits); }
+// a quiet NaN whose low kBoxBits bits index the instance's own value of that
+// entry (batch_family.h).  Input data is checked finite at set-up, so no
+// genuine value is a NaN.
 __device__ __forceinline__ float nan_box(float, uint32_t t) { return __uint_as_float(0x7FC00000u | t); }
 __device__ __forceinline__ double nan_box(double, uint32_t t) {
   return __longlong_as_double((long long)(0x7FF8000000000000ull | (unsigned long long)t));
@@ -1856,92 +1855,6 @@ KernelOf<T> products_kernel_for(int block, const Smem &sm) {
     case kStageGlobalSG: return products_kernel_mode<T, kStageGlobalSG>(block);
     default: return products_kernel_mode<T, kStageGlobal>(block);
   }
-}
-
-// Instances of one wave that share a pattern (sizes, cone table, Ap, Ai)
-// and whose values differ only at a few positions: `vary` marks, per CSC
-// position, where any member's value differs from the first member's.
-struct FamilyGroup {
-  std::vector<int64_t> members;
-  std::vector<uint8_t> vary;
-  int64_t nvary = 0;
-};
-
-// 64-bit mix of a problem's shape, cones and a sample of its pattern (a
-// filter: equality is checked exactly afterwards).
-inline uint64_t pattern_hash(const pdosgpu_problem &p) {
-  uint64_t h = 0x9E3779B97F4A7C15ull;
-  auto mix = [&](uint64_t v) {
-    h ^= v + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
-    h *= 0xBF58476D1CE4E5B9ull;
-  };
-  mix((uint64_t)p.m);
-  mix((uint64_t)p.n);
-  mix((uint64_t)p.f);
-  mix((uint64_t)p.l);
-  mix((uint64_t)p.qsize);
-  for (int64_t k = 0; k < p.qsize; ++k) mix((uint64_t)p.q[k]);
-  constexpr int64_t kStride = 61;  // every 61st entry of Ap and Ai, and the last
-  for (int64_t j = 0; j <= p.n; j += kStride) mix((uint64_t)p.Ap[j]);
-  mix((uint64_t)p.Ap[p.n]);
-  const int64_t nz = p.Ap[p.n];
-  for (int64_t k = 0; k < nz; k += kStride) mix((uint64_t)p.Ai[k]);
-  if (nz > 0) mix((uint64_t)p.Ai[nz - 1]);
-  return h;
-}
-
-inline bool same_pattern(const pdosgpu_problem &a, const pdosgpu_problem &b) {
-  if (a.m != b.m || a.n != b.n || a.f != b.f || a.l != b.l || a.qsize != b.qsize) return false;
-  if (a.qsize > 0 && std::memcmp(a.q, b.q, sizeof(int64_t) * a.qsize) != 0) return false;
-  if (std::memcmp(a.Ap, b.Ap, sizeof(int64_t) * (a.n + 1)) != 0) return false;
-  const int64_t nz = a.Ap[a.n];
-  return nz == 0 || std::memcmp(a.Ai, b.Ai, sizeof(int64_t) * nz) == 0;
-}
-
-// Family groups of at least two instances whose varying positions are at
-// most a quarter of the nonzeros (and few enough for the NaN boxes).
-inline std::vector<FamilyGroup> find_family_groups(const pdosgpu_problem *probs, int64_t cnt) {
-  std::vector<FamilyGroup> out;
-  if (cnt < 2) return out;
-  std::vector<uint64_t> key(cnt);
-  parallel_for(cnt, [&](int64_t i) { key[i] = pattern_hash(probs[i]); });
-  std::vector<int64_t> order(cnt);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
-  std::vector<std::vector<int64_t>> cand;
-  for (int64_t s0 = 0; s0 < cnt;) {
-    int64_t s1 = s0 + 1;
-    while (s1 < cnt && key[order[s1]] == key[order[s0]]) ++s1;
-    if (s1 - s0 >= 2) {
-      std::vector<int64_t> mem(order.begin() + s0, order.begin() + s1);
-      std::sort(mem.begin(), mem.end());
-      cand.push_back(std::move(mem));
-    }
-    s0 = s1;
-  }
-  for (auto &mem : cand) {
-    const pdosgpu_problem &r = probs[mem[0]];
-    std::vector<uint8_t> same(mem.size(), 1);
-    parallel_for((int64_t)mem.size(), [&](int64_t k) { same[k] = same_pattern(r, probs[mem[k]]) ? 1 : 0; });
-    FamilyGroup fg;
-    for (size_t k = 0; k < mem.size(); ++k)
-      if (same[k]) fg.members.push_back(mem[k]);
-    if (fg.members.size() < 2) continue;
-    const int64_t nz = r.Ap[r.n];
-    fg.vary.assign(nz > 0 ? nz : 1, 0);
-    const int64_t chunk = 4096, nchunks = (nz + chunk - 1) / chunk;
-    parallel_for(nchunks, [&](int64_t c) {
-      const int64_t k0 = c * chunk, k1 = std::min(nz, k0 + chunk);
-      for (size_t k = 1; k < fg.members.size(); ++k) {
-        const double *a = probs[fg.members[k]].Ax;
-        for (int64_t e = k0; e < k1; ++e)
-          if (a[e] != r.Ax[e]) fg.vary[e] = 1;
-      }
-    });
-    for (int64_t e = 0; e < nz; ++e) fg.nvary += fg.vary[e];
-    if (fg.nvary * 4 <= nz && box_index_fits(fg.nvary)) out.push_back(std::move(fg));
-  }
-  return out;
 }
 
 class BatchBase {
