@@ -1251,13 +1251,19 @@ __global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_pair_products_kerne
 // memory through distributed shared memory, in rank order, so every thread
 // of the cluster holds the same totals.  Per-row sums are those of the
 // one-CTA kernel; only the order of the block sums differs.
-// The cluster size is chosen at launch: 4 CTAs for a batch's class (more
-// clusters fit the device at once -- its GPCs hold 16 of their SMs in 8-CTA
-// clusters -- and a cluster synchronises fewer CTAs), 8 for pdos() on one
-// instance, which has the device to itself.
-constexpr int kClusterMax = 8;       // portable cluster size limit
-constexpr int kClusterCtasBatch = 4;
+// The cluster size is chosen at launch (cluster_ctas_for): a class of many
+// instances runs on 2-CTA clusters (more clusters fit the device at once --
+// its GPCs hold only 16 of their SMs in 8-CTA clusters -- and a cluster
+// synchronises fewer CTAs), a class of few on 4 or 8, so that its instances
+// still spread over the device; pdos() on one instance takes 8.
+constexpr int kClusterMax = 8;  // portable cluster size limit
 constexpr int kClusterCtasOne = 8;
+inline int cluster_ctas_for(int members, int sms, bool one_instance) {
+  if (one_instance) return kClusterCtasOne;
+  if (members >= sms / 2) return 2;
+  if (members >= sms / 4) return 4;
+  return 8;
+}
 
 __device__ __forceinline__ int cluster_ctas() {
   uint32_t n;
@@ -1956,7 +1962,7 @@ class BatchEngine : public BatchBase {
   std::vector<cudaGraphExec_t> exec_;  // [0]: one launch of iter_cap iterations
   int iter_cap_ = 64;
   int gregions_ = 0;  // staging regions allocated for the global class
-  int cluster_ctas_ = kClusterCtasBatch;  // CTAs per cluster of the global class
+  int cluster_ctas_ = kClusterCtasOne;  // CTAs per cluster of the global class
   Dev<T> dev_{};
   Inst *inst_d_ = nullptr;
   State *state_d_ = nullptr;
@@ -2504,7 +2510,7 @@ int BatchEngine<T>::commit() {
   B.gscratch = nullptr;
   {  // one staging region per resident CTA (at most 8 per SM) or cluster of the global class
     const int members_g = class_begin_h_[kGlobalClass + 1] - class_begin_h_[kGlobalClass];
-    cluster_ctas_ = opt_.batch_clusters ? kClusterCtasOne : kClusterCtasBatch;
+    cluster_ctas_ = cluster_ctas_for(members_g, num_sms(), opt_.batch_clusters != 0);
     gregions_ = on_clusters(smem_[kGlobalClass]) ? std::min(members_g, std::max(1, num_sms() / cluster_ctas_))
                                                  : std::min(members_g, num_sms() * (1024 / kBlocks[0]));
     if (gregions_ > 0) PDOS_TRY(arena_.alloc(&B.gscratch, (size_t)gregions_ * smem_[kGlobalClass].stride()));
