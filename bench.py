@@ -614,7 +614,7 @@ def run_batch_waves(args, wl):
     achieved = roof_bytes / (solve_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": "batch_admm_kernel / batch_cluster_kernel (whole fused ADMM "
                                           "iteration per CTA; instances too large for one CTA's shared "
-                                          "memory on a 4-CTA cluster)",
+                                          "memory on a cluster of 2 to 8 CTAs)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_kind": peak_kind, "traffic": batch_traffic(args.workload, roof_bytes, "batch_cluster_kernel"),
                 "algorithmic_bytes_of_solve": roof_bytes, "ms_of_solve": solve_ms,

@@ -60,7 +60,8 @@ typedef struct {
                          [4, 1024]) */
   int batch_piece;    /* batches only: nonzeros per piece at most (0: 1,024;
                          else a multiple of 4 in [64, 16384]) */
-  int batch_clusters; /* batches only: 0 (default) runs on 4-CTA clusters only
+  int batch_clusters; /* batches only: 0 (default) runs on clusters of 2 to 8
+                         CTAs (fewer CTAs when there are more of them) only
                          the instances too large for one CTA's shared memory;
                          1 runs every instance whose gather vector fits
                          shared memory on an 8-CTA cluster */

@@ -398,7 +398,7 @@ def _cluster_batch():
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_large_instances_on_clusters_match_single_instance_solves(built_lib, torch_cuda, precision):
-    """Instances of the global-staging class run on 4-CTA clusters (rows
+    """Instances of the global-staging class run on thread-block clusters (rows
     shared among the cluster's warps, sums met through distributed shared
     memory); each must match its single-instance solve as the one-CTA batch
     does, and a repeated solve must give the same bits."""
