@@ -302,9 +302,13 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
   int64_t *cone_off = nullptr, *cone_len = nullptr;
   if (ncones > 0) {
     cone_of_row_h.assign(m, -1);
-    batch::parallel_for(ncones, [&](int64_t c) {
+    auto fill = [&](int64_t c) {
       for (int64_t i = 0; i < d.soc_len[c]; ++i) cone_of_row_h[d.soc_off[c] + i] = (int32_t)c;
-    });
+    };
+    if (ninst > 1)  // a batch: cones of many instances, in parallel
+      batch::parallel_for(ncones, fill);
+    else
+      for (int64_t c = 0; c < ncones; ++c) fill(c);
     PDOS_TRY(tmp.alloc(&cone_of_row, (size_t)m));
     PDOS_TRY(tmp.alloc(&cone_off, (size_t)ncones));
     PDOS_TRY(tmp.alloc(&cone_len, (size_t)ncones));
@@ -470,7 +474,7 @@ int setup_problem(const ProblemDesc &d, DeviceArena &arena, cudaStream_t st, Dev
   P.ap_host.assign((size_t)n + 1, 0);
   PDOS_CUDA_TRY(cudaMemcpyAsync(P.rp_host.data(), P.Rp, sizeof(int32_t) * (m + 1), cudaMemcpyDeviceToHost, st));
   PDOS_CUDA_TRY(cudaStreamSynchronize(st));
-  batch::parallel_for((n + 1 + 65535) / 65536, [&](int64_t c) {
+  batch::parallel_for((n + 1 + 65535) / 65536, [&](int64_t c) {  // one chunk (no thread) below 65,536
     for (int64_t j = c * 65536; j < std::min<int64_t>(n + 1, (c + 1) * 65536); ++j) P.ap_host[j] = (int32_t)d.Ap[j];
   });
   tmp.release();

@@ -117,3 +117,15 @@ def test_batch_marshalling_matches_one_by_one():
     assert len(a) == len(b)
     for x, y in zip(a, b):
         assert bytes(x) == bytes(y)
+
+
+def test_library_dir_override(monkeypatch, tmp_path):
+    """PDOS_GB300_LIB_DIR points the loader at a side-by-side build; an
+    empty value means the in-tree one."""
+    from pdos_gb300 import _lib
+    monkeypatch.setenv("PDOS_GB300_LIB_DIR", str(tmp_path))
+    assert _lib.lib_file() == os.path.join(str(tmp_path), "libpdosindir.so")
+    monkeypatch.setenv("PDOS_GB300_LIB_DIR", "")
+    assert _lib.lib_file() == os.path.join(_lib.LIB_DIR, "libpdosindir.so")
+    monkeypatch.delenv("PDOS_GB300_LIB_DIR")
+    assert _lib.lib_file("libpdosindir_i32.so") == os.path.join(_lib.LIB_DIR, "libpdosindir_i32.so")
