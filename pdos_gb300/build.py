@@ -35,14 +35,18 @@ UNITS = [
     ("engine.o", "engine.cu", ["-DPDOS_DLONG"]),
     ("api.o", "api.cu", ["-DPDOS_DLONG"]),
     ("batch.o", "batch.cu", ["-DPDOS_DLONG"]),
+    ("batch_f32.o", "batch_f32.cu", ["-DPDOS_DLONG"]),
+    ("batch_f64.o", "batch_f64.cu", ["-DPDOS_DLONG"]),
     ("mlp.o", "mlp.cu", ["-DPDOS_DLONG"]),
     ("noalloc.o", "noalloc.cu", ["-DPDOS_DLONG"]),
     ("abi_l.o", "abi.cu", ["-DPDOS_DLONG"]),
     ("abi_i.o", "abi.cu", []),
 ]
 TARGETS = {
-    "libpdosindir.so": ["engine.o", "api.o", "batch.o", "mlp.o", "noalloc.o", "abi_l.o"],
-    "libpdosindir_i32.so": ["engine.o", "api.o", "batch.o", "mlp.o", "noalloc.o", "abi_i.o"],
+    "libpdosindir.so": ["engine.o", "api.o", "batch.o", "batch_f32.o", "batch_f64.o", "mlp.o", "noalloc.o",
+                        "abi_l.o"],
+    "libpdosindir_i32.so": ["engine.o", "api.o", "batch.o", "batch_f32.o", "batch_f64.o", "mlp.o", "noalloc.o",
+                            "abi_i.o"],
 }
 # C programs linked against the libraries: (executable, library, C flags)
 PROGRAMS = [

@@ -1,5 +1,5 @@
 // Family groups of a batch set-up wave (host only, CUDA-free; used by
-// batch.cu and checked on the CPU): instances whose sizes, cone table and
+// batch_engine.cuh and checked on the CPU): instances whose sizes, cone table and
 // sparsity pattern (Ap, Ai) are identical and whose values differ at no more
 // than a quarter of the nonzeros share one matrix layout.  At a varying
 // entry the shared value array holds a quiet NaN whose low kBoxBits bits

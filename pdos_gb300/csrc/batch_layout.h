@@ -1,7 +1,7 @@
 // Host-side builder of the batch solver's hybrid matrix layout (no CUDA):
 // for every instance and each side of it (rows of A, rows of A'), slices of
 // 32 rows stored column-major and long rows cut into warp-wide pieces, with
-// instance-local 16-bit gather indices.  Used by batch.cu and tested on the
+// instance-local 16-bit gather indices.  Used by batch_engine.cuh and tested on the
 // CPU.
 #pragma once
 
