@@ -34,8 +34,10 @@ JSON line (rank 0):
            a few held-out instances from the cold start
 --impl reference runs that CPU solver on all host cores instead.
 Other workloads (--workload): the single-instance configurations
-(portfolio_n200k_fp64, portfolio_n100_fp64, random_socp_m600k_fp32) and a
-batch of uneven portfolio instances (portfolio_mix_batch).
+(portfolio_n200k_fp64 and its random-cone-split twin
+portfolio_n200k_split_fp64, portfolio_n100_fp64, random_socp_m600k_fp32),
+batches of uneven portfolio instances (portfolio_mix_batch, n <= 2,000; and
+portfolio_uneven_full, n up to 20,000 at full size, set up in waves).
 Multi-GPU (torchrun): batch workloads shard the instances across ranks (no
 collective); single-instance workloads run replicas.
 """
@@ -62,6 +64,13 @@ WORKLOADS = {
                                  precision="fp64", iters_per_solve=1700,
                                  params=dict(EPS_ABS=1e-4, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4,
                                              MAX_ITERS=2000, NORMALIZE=0)),
+    # the same instance with its second-order cone cut into cones of random
+    # sizes U[2, 64] (6,126 small cones instead of one of 202,001 rows); it
+    # reaches EPS 1e-4 in 1358 ADMM iterations on the FP64 path
+    "portfolio_n200k_split_fp64": dict(gen="portfolio", n=200_000, k=2_000, density=0.05, seed=1,
+                                       soc_split=True, precision="fp64", iters_per_solve=1358,
+                                       params=dict(EPS_ABS=1e-4, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4,
+                                                   MAX_ITERS=2000, NORMALIZE=0)),
     # the small CPU-runnable case
     "portfolio_n100_fp64": dict(gen="portfolio", n=100, k=10, density=0.5, seed=0, precision="fp64",
                                 params=dict(EPS_ABS=5e-3, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4,
@@ -99,7 +108,8 @@ DEFAULT_WORKLOAD = "portfolio_family_warmstart"
 def make_problem(wl):
     from pdos_gb300.generators import portfolio, random_feasible
     if wl["gen"] == "portfolio":
-        return portfolio(wl["n"], wl["k"], wl["density"], seed=wl["seed"], params=wl["params"])
+        return portfolio(wl["n"], wl["k"], wl["density"], seed=wl["seed"], params=wl["params"],
+                         random_soc_split=wl.get("soc_split", False))
     return random_feasible(wl["m"], wl["n"], wl["nnz_per_col"], seed=wl["seed"], params=wl["params"])
 
 
