@@ -100,7 +100,10 @@ BATCH_WORKLOADS = {
     # (about 1.1e10 nonzeros), generated on the host cores and set up on the
     # device in waves of 256 instances, never all on the host at once
     "portfolio_uneven_full": dict(kind="mix_waves", batch=4096, n_lo=50, n_hi=20000, density=0.2, seed=3,
-                                  precision="fp32", params=_BATCH_PARAMS, wave=256),
+                                  precision="fp32", params=_BATCH_PARAMS, wave=256,
+                                  # mean ADMM iterations of each n-decile in the batch's cold solve
+                                  # (measured on one GB300), for the reference arm's extrapolation
+                                  iters_by_decile=[291, 417, 491, 583, 636, 702, 758, 811, 865, 912]),
 }
 DEFAULT_WORKLOAD = "portfolio_family_warmstart"
 
@@ -504,6 +507,8 @@ def run_batch_reference(args, wl):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    if wl["kind"] == "mix_waves":
+        return run_uneven_reference(args, wl)
     from oracle import oracle as O
     O.build_port()
     cores = os.cpu_count() or 1
@@ -525,6 +530,67 @@ def run_batch_reference(args, wl):
                                                  "params": wl["params"]},
         "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
                          "sample": f"{cores} processes x 1 held-out instance per step (cold start)"},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def decile_samples(sizes):
+    """n-decile of every instance and the first instance of each decile."""
+    ns = np.array([n for n, _ in sizes])
+    edges = np.quantile(ns, np.linspace(0, 1, 11))
+    decile = np.clip(np.searchsorted(edges, ns, side="right") - 1, 0, 9)
+    samples = {int(np.nonzero(decile == d)[0][0]): d for d in range(10) if (decile == d).any()}
+    return ns, decile, samples
+
+
+def _cpu_gen_iter_sample(job):
+    n, k, density, seed, params, iters = job
+    from pdos_gb300 import generators as g
+    return cpu_sample(g.portfolio(n, k, density, seed=seed, params=params), iters)
+
+
+def run_uneven_reference(args, wl):
+    """--impl reference on the full-size uneven batch, where one reference
+    solve of the largest instances takes minutes: every step times the
+    oracle (1 thread per process, all host cores) on one instance per
+    n-decile, set-up plus --cpu-iters ADMM iterations, and extrapolates each
+    decile with its measured mean iteration count (iters_by_decile); the
+    value is the batch's instances over the summed solve time, spread over
+    the cores."""
+    import multiprocessing as mp
+    from pdos_gb300 import generators as g
+    from oracle import oracle as O
+    O.build_port()
+    count = args.batch or wl["batch"]
+    sizes = g.portfolio_batch_sizes(count, wl["n_lo"], wl["n_hi"], seed=wl["seed"])
+    seed0 = wl["seed"] * 1_000_003
+    ns, decile, samples = decile_samples(sizes)
+    ids = sorted(samples)
+    jobs = [(sizes[i][0], sizes[i][1], wl["density"], seed0 + i, wl["params"], args.cpu_iters) for i in ids]
+    cores = os.cpu_count() or 1
+    rates = []
+    with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
+        for _ in range(args.warmup + args.steps):
+            res = pool.map(_cpu_gen_iter_sample, jobs, chunksize=1)
+            total = 0.0
+            for i, (ts, ti) in zip(ids, res):
+                d = samples[i]
+                total += (ts + ti * wl["iters_by_decile"][d]) * int((decile == d).sum())
+            rates.append(cores * count / total)
+    val = float(np.median(rates[args.warmup:]))
+    line = {
+        "impl": "reference", "metric": batch_metric(wl), "value": val, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * count / val,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": {"workload": args.workload, "instances_per_step": count,
+                                                 "n_range": [wl["n_lo"], wl["n_hi"]], "params": wl["params"]},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"oracle on {len(jobs)} instances (one per n-decile) per step, set-up + "
+                                   f"{args.cpu_iters} ADMM iterations each, extrapolated with each decile's "
+                                   f"measured mean iteration count, weighted by its instances, spread over "
+                                   f"{cores} cores"},
         "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -569,10 +635,7 @@ def run_batch_waves(args, wl):
     seed0 = wl["seed"] * 1_000_003
     jobs = [(n, k, wl["density"], seed0 + i, wl["params"]) for i, (n, k) in enumerate(sizes)]
     shapes = [_portfolio_shape(n, k, wl["density"]) for n, k in sizes]
-    ns = np.array([n for n, _ in sizes])
-    edges = np.quantile(ns, np.linspace(0, 1, 11))
-    decile = np.clip(np.searchsorted(edges, ns, side="right") - 1, 0, 9)
-    samples = {int(np.nonzero(decile == d)[0][0]): d for d in range(10) if (decile == d).any()}
+    ns, decile, samples = decile_samples(sizes)
     kept = {}
     cores = os.cpu_count() or 2
     pool = mp.get_context("spawn").Pool(max(1, cores - 1))

@@ -62,3 +62,16 @@ def test_reference_arm_other_ranks_print_nothing():
     out = _run(["--impl", "reference", "--steps", "1", "--warmup", "0"],
                env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert not [l for l in out.splitlines() if l.startswith("{")]
+
+
+def test_reference_arm_uneven_full_is_bounded():
+    """The full-size uneven batch: one instance per n-decile, a few ADMM
+    iterations each, extrapolated (a full reference solve of the largest
+    instances takes minutes)."""
+    d = _line(_run(["--workload", "portfolio_uneven_full", "--impl", "reference", "--steps", "1",
+                    "--warmup", "0", "--batch", "64"]))
+    _check_common(d)
+    assert d["metric"].startswith("solves/s at EPS_ABS 1e-4: batched uneven instances")
+    assert d["config"]["workload"] == "portfolio_uneven_full"
+    assert d["config"]["instances_per_step"] == 64
+    assert "one per n-decile" in d["cpu_baseline"]["sample"]
