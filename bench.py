@@ -80,7 +80,7 @@ WORKLOADS = {
     # family (1,307 at m = 6,000, 3,789 at m = 30,000) and does not converge
     # with NORMALIZE=1 within 4,000
     "random_socp_m600k_fp32": dict(gen="random", m=600_000, n=200_000, nnz_per_col=20, seed=2,
-                                   precision="fp32",
+                                   precision="fp32", iters_per_solve=3146,  # the GPU solve's count
                                    params=dict(EPS_ABS=1e-4, ALPHA=1.0, CG_MAX_ITS=20, CG_TOL=1e-4,
                                                MAX_ITERS=30000, NORMALIZE=0)),
 }
