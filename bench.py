@@ -551,6 +551,44 @@ def _cpu_gen_iter_sample(job):
     return cpu_sample(g.portfolio(n, k, density, seed=seed, params=params), iters)
 
 
+def stratified_cpu_estimate(wl, sizes, iters_of, per_decile, cpu_iters, pool, seed=7):
+    """The oracle's time for a whole uneven batch, from a seeded stratified
+    subsample: up to `per_decile` instances of every n-decile (regenerated
+    from their seeds in the pool's processes), each timed for set-up plus
+    `cpu_iters` ADMM iterations and extrapolated to `iters_of(i, d)`
+    iterations; a decile's mean time counts once per instance of the decile.
+    Returns (total seconds, per-decile summary, instances sampled)."""
+    ns, decile, _ = decile_samples(sizes)
+    rng = np.random.default_rng(seed)
+    picks = []
+    for d in range(10):
+        members = np.nonzero(decile == d)[0]
+        if len(members) == 0:
+            continue
+        take = members if len(members) <= per_decile else np.sort(rng.choice(members, per_decile, replace=False))
+        picks += [(int(i), d) for i in take]
+    seed0 = wl["seed"] * 1_000_003
+    jobs = [(sizes[i][0], sizes[i][1], wl["density"], seed0 + i, wl["params"], cpu_iters) for i, _ in picks]
+    res = pool.map(_cpu_gen_iter_sample, jobs, chunksize=1)
+    times = {d: [] for d in range(10)}
+    steps = {d: [] for d in range(10)}
+    for (i, d), (ts, ti) in zip(picks, res):
+        it = float(iters_of(i, d))
+        times[d].append(ts + ti * it)
+        steps[d].append(ti)
+    total, per = 0.0, {}
+    for d in range(10):
+        if not times[d]:
+            continue
+        members = int((decile == d).sum())
+        total += float(np.mean(times[d])) * members
+        per[d] = {"instances": members, "sampled": len(times[d]),
+                  "n_range": [int(ns[decile == d].min()), int(ns[decile == d].max())],
+                  "mean_seconds_per_solve": float(np.mean(times[d])),
+                  "mean_s_per_admm_iteration": float(np.mean(steps[d]))}
+    return total, per, len(picks)
+
+
 def run_uneven_reference(args, wl):
     """--impl reference on the full-size uneven batch, where one reference
     solve of the largest instances takes minutes: every step times the
@@ -565,19 +603,13 @@ def run_uneven_reference(args, wl):
     O.build_port()
     count = args.batch or wl["batch"]
     sizes = g.portfolio_batch_sizes(count, wl["n_lo"], wl["n_hi"], seed=wl["seed"])
-    seed0 = wl["seed"] * 1_000_003
-    ns, decile, samples = decile_samples(sizes)
-    ids = sorted(samples)
-    jobs = [(sizes[i][0], sizes[i][1], wl["density"], seed0 + i, wl["params"], args.cpu_iters) for i in ids]
     cores = os.cpu_count() or 1
     rates = []
-    with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
-        for _ in range(args.warmup + args.steps):
-            res = pool.map(_cpu_gen_iter_sample, jobs, chunksize=1)
-            total = 0.0
-            for i, (ts, ti) in zip(ids, res):
-                d = samples[i]
-                total += (ts + ti * wl["iters_by_decile"][d]) * int((decile == d).sum())
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            total, _, sampled = stratified_cpu_estimate(
+                wl, sizes, lambda i, d: wl["iters_by_decile"][d], args.cpu_per_decile, args.cpu_iters, pool,
+                seed=7 + step)
             rates.append(cores * count / total)
     val = float(np.median(rates[args.warmup:]))
     line = {
@@ -587,10 +619,10 @@ def run_uneven_reference(args, wl):
         "data": "synthetic (seeded)", "config": {"workload": args.workload, "instances_per_step": count,
                                                  "n_range": [wl["n_lo"], wl["n_hi"]], "params": wl["params"]},
         "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"oracle on {len(jobs)} instances (one per n-decile) per step, set-up + "
-                                   f"{args.cpu_iters} ADMM iterations each, extrapolated with each decile's "
-                                   f"measured mean iteration count, weighted by its instances, spread over "
-                                   f"{cores} cores"},
+                         "sample": f"oracle on a stratified subsample of {sampled} instances (up to "
+                                   f"{args.cpu_per_decile} per n-decile) per step, set-up + {args.cpu_iters} "
+                                   f"ADMM iterations each, extrapolated with each decile's measured mean "
+                                   f"iteration count, weighted by its instances, spread over {cores} cores"},
         "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -601,11 +633,6 @@ def _gen_mix_instance(job):
     n, k, density, seed, params = job
     from pdos_gb300 import generators as g
     return g.portfolio(n, k, density, seed=seed, params=params)
-
-
-def _cpu_iter_sample(job):
-    prob, iters = job
-    return cpu_sample(prob, iters)
 
 
 def _portfolio_shape(n, k, density):
@@ -698,29 +725,22 @@ def run_batch_waves(args, wl):
     iters = np.array([d["admm_iters"] for d in inf])
     starts_x = np.concatenate([[0], np.cumsum([sh[0] for sh in shapes])])
 
-    # CPU baseline: the oracle (1 core per process) on one instance per
-    # n-decile, set-up plus a few ADMM iterations, extrapolated with the
-    # iteration count the GPU solve needed for that instance and weighted by
-    # the instances of its decile
+    # CPU baseline: the oracle (1 core per process) on a seeded stratified
+    # subsample (up to --cpu-per-decile instances per n-decile), set-up plus
+    # a few ADMM iterations each, extrapolated with the iteration count the
+    # GPU solve needed for that instance and weighted by the instances of
+    # its decile
     cpu = None
     if not args.no_cpu:
-        sample_ids = sorted(kept)
         t0 = time.perf_counter()
-        res = pool.map(_cpu_iter_sample, [(kept[i], args.cpu_iters) for i in sample_ids], chunksize=1)
+        total, per, sampled = stratified_cpu_estimate(wl, sizes, lambda i, d: iters[i], args.cpu_per_decile,
+                                                      args.cpu_iters, pool)
         cpu_secs = time.perf_counter() - t0
-        total = 0.0
-        per = {}
-        for i, (ts, ti) in zip(sample_ids, res):
-            d = samples[i]
-            members = np.nonzero(decile == d)[0]
-            t_inst = ts + ti * float(np.mean(iters[members]))
-            total += t_inst * len(members)
-            per[int(d)] = {"n": int(ns[i]), "setup_s": ts, "s_per_admm_iteration": ti,
-                           "admm_iterations_mean_of_decile": float(np.mean(iters[members]))}
         cpu = {"value": count / total, "unit": "solves/s", "cores": 1, "kind": "port",
-               "sample": f"oracle (C restatement, 1 core per process): one instance per n-decile, set-up + "
-                         f"{args.cpu_iters} ADMM iterations, extrapolated with the decile's mean GPU "
-                         f"iteration count and weighted by its instances ({cpu_secs:.0f} s of sampling)",
+               "sample": f"oracle (C restatement, 1 core per process): a stratified subsample of {sampled} "
+                         f"instances (up to {args.cpu_per_decile} per n-decile), set-up + {args.cpu_iters} "
+                         f"ADMM iterations each, extrapolated with that instance's GPU iteration count and "
+                         f"weighted by its decile's instances ({cpu_secs:.0f} s of sampling)",
                "deciles": per}
     pool.close()
     pool.join()
@@ -1141,6 +1161,8 @@ def main():
                     help="held-out instances checked against the FP64 oracle at EPS_ABS 1e-8 "
                          "(batch workloads)")
     ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--cpu-per-decile", type=int, default=64,
+                    help="full-size uneven batch: instances per n-decile in the CPU baseline's subsample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--own-layouts", action="store_true",

@@ -65,13 +65,13 @@ def test_reference_arm_other_ranks_print_nothing():
 
 
 def test_reference_arm_uneven_full_is_bounded():
-    """The full-size uneven batch: one instance per n-decile, a few ADMM
-    iterations each, extrapolated (a full reference solve of the largest
-    instances takes minutes)."""
+    """The full-size uneven batch: a stratified subsample (here 2 instances
+    per n-decile), a few ADMM iterations each, extrapolated (a full reference
+    solve of the largest instances takes minutes)."""
     d = _line(_run(["--workload", "portfolio_uneven_full", "--impl", "reference", "--steps", "1",
-                    "--warmup", "0", "--batch", "64"]))
+                    "--warmup", "0", "--batch", "64", "--cpu-per-decile", "2"]))
     _check_common(d)
     assert d["metric"].startswith("solves/s at EPS_ABS 1e-4: batched uneven instances")
     assert d["config"]["workload"] == "portfolio_uneven_full"
     assert d["config"]["instances_per_step"] == 64
-    assert "one per n-decile" in d["cpu_baseline"]["sample"]
+    assert "stratified subsample of 20 instances" in d["cpu_baseline"]["sample"]
