@@ -203,7 +203,8 @@ class Batch:
         self._totals()
 
     @classmethod
-    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0, share_layouts=True, layout=None):
+    def in_waves(cls, waves, precision="fp64", device=0, iters_per_launch=0, share_layouts=True, layout=None,
+                 clusters=False):
         """A batch set up from an iterable of problem lists, one
         pdosgpu_batch_append per list, so that only one list has to exist on
         the host at a time (pdosgpu_batch_create / append / commit).  Keeps
@@ -212,7 +213,7 @@ class Batch:
         self.lib = _lib.load()
         self.probs = None
         self.sizes = []
-        self._opt = make_options(precision, "2norm", device, share_layouts, layout=layout)
+        self._opt = make_options(precision, "2norm", device, share_layouts, layout=layout, clusters=clusters)
         self._b = ctypes.c_void_p()
         _lib.check(self.lib.pdosgpu_batch_create(ctypes.byref(self._opt), int(iters_per_launch),
                                                  ctypes.byref(self._b)), "pdosgpu_batch_create", self.lib)
