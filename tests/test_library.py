@@ -129,3 +129,21 @@ def test_library_dir_override(monkeypatch, tmp_path):
     assert _lib.lib_file() == os.path.join(_lib.LIB_DIR, "libpdosindir.so")
     monkeypatch.delenv("PDOS_GB300_LIB_DIR")
     assert _lib.lib_file("libpdosindir_i32.so") == os.path.join(_lib.LIB_DIR, "libpdosindir_i32.so")
+
+
+def test_make_options_maps_python_names_to_the_c_options(built_lib):
+    """make_options fills pdosgpu_options from the library's defaults and
+    rejects unknown names before any GPU call."""
+    from pdos_gb300 import _lib
+    from pdos_gb300.solver import make_options
+    d = make_options()
+    assert d.precision == _lib.PDOSGPU_FP64 and d.scaling == _lib.PDOSGPU_SCALE_2NORM
+    assert d.batch_layouts == _lib.PDOSGPU_BATCH_SHARE and d.engine == _lib.PDOSGPU_ENGINE_AUTO
+    assert d.batch_long_row == 0 and d.batch_piece == 0 and d.batch_clusters == 0
+    o = make_options("fp32", "ruiz", 0, share_layouts=False, engine="cluster", layout=(64, 512), clusters=True)
+    assert o.precision == _lib.PDOSGPU_FP32 and o.scaling == _lib.PDOSGPU_SCALE_RUIZ
+    assert o.batch_layouts == _lib.PDOSGPU_BATCH_OWN and o.engine == _lib.PDOSGPU_ENGINE_CLUSTER
+    assert (o.batch_long_row, o.batch_piece, o.batch_clusters) == (64, 512, 1)
+    for bad in (dict(precision="fp16"), dict(scaling="max"), dict(engine="warp")):
+        with pytest.raises(ValueError):
+            make_options(**bad)
