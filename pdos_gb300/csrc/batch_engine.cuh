@@ -74,6 +74,7 @@ struct HybPtr {
   const int32_t *split_row, *split_p0, *split_np;  // pieces of each split row
   const uint16_t *idx;         // gather index, local to the instance (< 65,536)
   const void *val;             // values (float or double)
+  const uint16_t *slice_row;   // row of each lane of a sorted instance's slices (NULL if none sorted)
 };
 
 struct Inst {
@@ -342,7 +343,8 @@ __device__ __forceinline__ void hyb_product_impl(const HybPtr &H, const Side &sd
         if (NV == 2) a1 = fma(v, src1[j], a1);
       }
     }
-    if (!((H.slice_skip[sk] >> lane) & 1u)) epi(s * 32 + lane, a0, a1);
+    if (!((H.slice_skip[sk] >> lane) & 1u))
+      epi(sd.sorted ? (int)H.slice_row[sk * 32 + lane] : s * 32 + lane, a0, a1);  // the lane's row
   }
   if (sd.nsplit > 0) {
     bar();
@@ -839,7 +841,8 @@ __device__ __forceinline__ void pair_product(const HybPtr &H, const Side &sd, co
         }
       }
     }
-    if (!((H.slice_skip[sk] >> lane) & 1u)) epi(s * 32 + lane, a0, a1);
+    if (!((H.slice_skip[sk] >> lane) & 1u))
+      epi(sd.sorted ? (int)H.slice_row[sk * 32 + lane] : s * 32 + lane, a0, a1);  // the lane's row
   }
   if (sd.nsplit > 0) {
     __syncthreads();
@@ -1699,7 +1702,8 @@ int upload_hyb(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStre
                int64_t *bytes) {
   *bytes += (int64_t)(hb.slice_beg.size() * 8 + hb.slice_w.size() * 4 + hb.slice_skip.size() * 4 +
                       hb.piece_row.size() * 4 + hb.piece_beg.size() * 8 + hb.piece_len.size() * 4 +
-                      hb.split_row.size() * 12 + hb.idx.size() * 2 + hb.src.size() * sizeof(T));
+                      hb.split_row.size() * 12 + hb.idx.size() * 2 + hb.src.size() * sizeof(T) +
+                      (hb.any_sorted ? hb.slice_row.size() * 2 : 0));
   auto up = [&](auto **dst, const auto &v) -> int {
     using E = typename std::decay_t<decltype(v)>::value_type;
     E *p = nullptr;
@@ -1723,6 +1727,8 @@ int upload_hyb(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStre
   PDOS_TRY(up(&split_p0, hb.split_p0));
   PDOS_TRY(up(&split_np, hb.split_np));
   PDOS_TRY(up(&idx, hb.idx));
+  uint16_t *slice_row = nullptr;
+  if (hb.any_sorted) PDOS_TRY(up(&slice_row, hb.slice_row));
   T *val = nullptr;
   PDOS_TRY(arena.alloc(&val, hb.src.size() + 1));
   if (!hb.src.empty()) {
@@ -1738,7 +1744,7 @@ int upload_hyb(const HybBuild &hb, const T *values, DeviceArena &arena, cudaStre
     PDOS_CUDA_TRY(cudaStreamSynchronize(st));  // before src (and the host arrays) are freed
   }
   h = HybPtr{slice_beg, slice_w, slice_skip, piece_row, piece_beg, piece_len, split_row, split_p0,
-             split_np, idx, val};
+             split_np, idx, val, slice_row};
   return PDOSGPU_OK;
 }
 

@@ -28,7 +28,13 @@ constexpr int kPiece = PDOS_BATCH_PIECE;    // default target nonzeros per piece
 struct Side {
   int64_t slice0, piece0, split0;
   int32_t nslices, npieces, nsplit, rows;
+  int32_t sorted;  // 1: the slices hold the short rows sorted by length (slice_row maps lanes to rows)
 };
+
+// Rows sorted by length inside windows of this many rows when an
+// instance's slices would otherwise pay more than kSortPadding of padding.
+constexpr int kSortWindow = 1024;
+constexpr double kSortPadding = 0.15;
 
 // Work over instances on the host's cores (atomic counter, no exceptions).
 template <class F>
@@ -72,12 +78,25 @@ struct Cursor {
 // instance (advances a cursor), walk<true> writes it at a cursor; both make
 // the same decisions, and every instance starts and ends on a multiple of
 // 4 elements, so instances can be sized and written in parallel.
+//
+// Slices hold an instance's short rows (at most long_row nonzeros) 32 at a
+// time, lane = row, padded to the slice's longest row.  In natural order a
+// slice also keeps a lane for each long row and each row past the end
+// (skipped).  When that order pays more than kSortPadding of padding and
+// sorting saves a tenth of the elements, the short rows are instead sorted
+// by length (longest first, stable) inside windows of kSortWindow rows and
+// packed densely; slice_row then gives each lane's row.  Each row keeps its
+// own entries in its own lane in their order, so its sum is the same chain
+// of fused multiply-adds either way.
 struct HybBuild {
   int long_row = kLongRow;  // rows with more nonzeros go to pieces (a multiple of 4, >= 4)
   int piece = kPiece;       // nonzeros per piece at most (a multiple of 4, >= 4)
+  bool sort_rows = true;    // let an instance with much padding sort its rows
   std::vector<int64_t> slice_beg;
   std::vector<int32_t> slice_w;
   std::vector<uint32_t> slice_skip;
+  std::vector<uint16_t> slice_row;  // [32 per slice] the row of each lane (sorted instances; else unused)
+  bool any_sorted = false;          // some instance of this build sorted its rows
   std::vector<int32_t> piece_row, piece_len, split_row, split_p0, split_np;
   std::vector<int64_t> piece_beg;
   Raw<uint16_t> idx;  // per element: local gather index
@@ -87,6 +106,7 @@ struct HybBuild {
     slice_beg.resize(t.slice);
     slice_w.resize(t.slice);
     slice_skip.resize(t.slice);
+    slice_row.assign((size_t)t.slice * 32, 0);
     piece_row.resize(t.piece);
     piece_len.resize(t.piece);
     piece_beg.resize(t.piece);
@@ -117,21 +137,55 @@ struct HybBuild {
     auto pad4 = [&]() {
       while (c.elem % 4) put(0, -1);  // zero entries up to 16-byte alignment
     };
-    for (int64_t s0 = 0; s0 < R; s0 += 32) {
+    // rows of the slices' lanes: natural order (lane = row, -1 for a long row
+    // or past the end) or, for an instance with much padding, its short rows
+    // sorted by length inside windows
+    auto len_of = [&](int64_t r) -> int64_t { return ptr[r0 + r + 1] - ptr[r0 + r]; };
+    auto slice_elems = [&](const std::vector<int32_t> &lanes) {
+      int64_t e = 0;
+      for (size_t s0 = 0; s0 < lanes.size(); s0 += 32) {
+        int64_t w = 0;
+        for (size_t k = s0; k < std::min(lanes.size(), s0 + 32); ++k)
+          if (lanes[k] >= 0) w = std::max(w, len_of(lanes[k]));
+        e += 32 * (w >= 4 ? (w + 3) & ~3 : w);
+      }
+      return e;
+    };
+    std::vector<int32_t> lanes((size_t)((R + 31) / 32 * 32), -1);
+    int64_t useful = 0;
+    for (int64_t r = 0; r < R; ++r)
+      if (len_of(r) <= long_row) {
+        lanes[r] = (int32_t)r;
+        useful += len_of(r);
+      }
+    if (sort_rows && R > 32) {
+      const int64_t natural = slice_elems(lanes);
+      if (natural - useful > kSortPadding * natural) {
+        std::vector<int32_t> sorted;
+        for (int64_t w0 = 0; w0 < R; w0 += kSortWindow) {
+          const size_t first = sorted.size();
+          for (int64_t r = w0; r < std::min<int64_t>(R, w0 + kSortWindow); ++r)
+            if (len_of(r) <= long_row) sorted.push_back((int32_t)r);
+          std::stable_sort(sorted.begin() + first, sorted.end(),
+                           [&](int32_t x, int32_t y) { return len_of(x) > len_of(y); });
+        }
+        sorted.resize((sorted.size() + 31) / 32 * 32, -1);
+        if (10 * slice_elems(sorted) < 9 * natural) {
+          lanes.swap(sorted);
+          sd.sorted = 1;
+        }
+      }
+    }
+    for (size_t s0 = 0; s0 < lanes.size(); s0 += 32) {
       uint32_t skip = 0;
       int width = 0;
       for (int lane = 0; lane < 32; ++lane) {
-        const int64_t r = s0 + lane;
-        if (r >= R) {
+        const int32_t r = lanes[s0 + lane];
+        if (r < 0) {
           skip |= 1u << lane;
           continue;
         }
-        const int len = ptr[r0 + r + 1] - ptr[r0 + r];
-        if (len > long_row) {
-          skip |= 1u << lane;
-          continue;
-        }
-        width = std::max(width, len);
+        width = std::max(width, (int)len_of(r));
       }
       const bool vec = width >= 4;
       if (vec) {
@@ -142,13 +196,15 @@ struct HybBuild {
         slice_beg[c.slice] = c.elem;
         slice_w[c.slice] = vec ? -width : width;
         slice_skip[c.slice] = skip;
+        for (int lane = 0; lane < 32; ++lane)
+          slice_row[(size_t)c.slice * 32 + lane] = (uint16_t)(lanes[s0 + lane] >= 0 ? lanes[s0 + lane] : 0);
       }
       for (int cidx = 0; cidx < width; cidx += vec ? 4 : 1) {
         for (int lane = 0; lane < 32; ++lane) {
           for (int t = 0; t < (vec ? 4 : 1); ++t) {
-            const int64_t r = s0 + lane;
+            const int32_t r = lanes[s0 + lane];
             int32_t j = 0, p = -1;
-            if (!((skip >> lane) & 1u)) {
+            if (r >= 0) {
               const int64_t a = ptr[r0 + r], len = ptr[r0 + r + 1] - a;
               if (cidx + t < len) {
                 p = (int32_t)(a + cidx + t);
@@ -226,6 +282,8 @@ void build_layout(HybBuild &hb, int64_t count, SideOf side, std::vector<Side> &o
     Cursor c = start[i];
     out[i] = hb.walk<true>(ptr, gidx, r0, r1, c0, c);
   });
+  hb.any_sorted = false;
+  for (const Side &sd : out) hb.any_sorted |= sd.sorted != 0;
 }
 
 }  // namespace batch

@@ -2,7 +2,8 @@
 // lays out the rows of seeded random block-diagonal matrices -- short rows,
 // rows of a few dozen entries, rows longer than a piece (split rows), empty
 // rows -- for many instances at once, sized and written in parallel as the
-// solver does, and checks every structural promise the kernels rely on.
+// solver does, and checks every structural promise the kernels rely on,
+// including the lane-to-row map of instances that sort their rows.
 // Prints "OK" and exits 0, or prints the first failures and exits 1.
 #include <cstdio>
 #include <random>
@@ -94,8 +95,12 @@ int main() {
       const int width = w < 0 ? -w : w;
       CHECK(beg + 32LL * width <= (int64_t)hb.idx.size(), "instance %d slice %d runs past the end", i, s);
       for (int lane = 0; lane < 32; ++lane) {
-        const int64_t r = 32LL * s + lane;
-        if ((hb.slice_skip[k] >> lane) & 1u) continue;
+        const int64_t r = sd.sorted ? (int64_t)hb.slice_row[(size_t)k * 32 + lane] : 32LL * s + lane;
+        if ((hb.slice_skip[k] >> lane) & 1u) {
+          // a sorted instance packs its short rows: only its last slice has skipped lanes
+          if (sd.sorted) CHECK(s == sd.nslices - 1, "instance %d: skipped lane inside sorted slice %d", i, s);
+          continue;
+        }
         CHECK(r < m, "instance %d slice %d: live lane past the last row", i, s);
         if (r >= m) continue;
         seen[r]++;
@@ -139,6 +144,44 @@ int main() {
     for (int64_t r = 0; r < m; ++r) CHECK(seen[r] == 1, "instance %d row %lld covered %d times", i, (long long)r, seen[r]);
   }
   CHECK(nsplit_total > 0, "no split rows were exercised");
+  // sorted instances: inside each window of rows, slice lanes hold rows in
+  // order of decreasing length
+  int nsorted = 0;
+  for (int i = 0; i < count; ++i) {
+    const Side &sd = sides[i];
+    if (!sd.sorted) continue;
+    ++nsorted;
+    int64_t prev_window = -1, prev_len = 0;
+    for (int64_t q = 0; q < 32LL * sd.nslices; ++q) {
+      const int64_t k = sd.slice0 + q / 32;
+      if ((hb.slice_skip[k] >> (q % 32)) & 1u) continue;
+      const int64_t r = hb.slice_row[(size_t)k * 32 + q % 32];
+      const int64_t len = ptr[r0[i] + r + 1] - ptr[r0[i] + r], window = r / kSortWindow;
+      CHECK(window >= prev_window, "instance %d: windows out of order", i);
+      if (window == prev_window) CHECK(len <= prev_len, "instance %d: rows not sorted by length", i);
+      prev_window = window;
+      prev_len = len;
+    }
+  }
+  CHECK(nsorted > 0, "no instance sorted its rows");
+  // the same matrices in natural row order take more elements
+  HybBuild nat;
+  nat.long_row = lp[0];
+  nat.piece = lp[1];
+  nat.sort_rows = false;
+  std::vector<Side> nsides;
+  build_layout<int32_t>(nat, count, [&](int64_t i, const int32_t *&p, const int32_t *&gi, int64_t &a, int64_t &b,
+                                        int64_t &c) {
+    p = ptr.data();
+    gi = col.data();
+    a = r0[i];
+    b = r0[i + 1];
+    c = c0[i];
+  }, nsides);
+  CHECK(!nat.any_sorted && hb.any_sorted, "sorting switch");
+  CHECK(hb.idx.size() < nat.idx.size(), "sorting did not shrink the layout");
+  std::printf("long_row %d, piece %d: %d of %d instances sorted, %zu elements against %zu in natural order "
+              "(%zu nonzeros)\n", lp[0], lp[1], nsorted, count, hb.idx.size(), nat.idx.size(), col.size());
   total_elems += (long long)hb.idx.size();
   }
   if (failures) {

@@ -7,7 +7,11 @@ does, and checks what the batch kernel relies on.  Every nonzero is placed
 exactly once, with its instance-local index.  Every row is covered exactly
 once: by a slice lane, by one piece, or by the pieces of a split record.
 Slices and pieces are 4-aligned and within their width and length limits,
-and padding is marked."""
+and padding is marked.  Instances whose natural row order pays much padding
+sort their short rows by length inside windows: their lanes map to rows
+through slice_row, only their last slice skips lanes, and their layouts are
+smaller than the natural-order ones (57 % padding down to about 6 % on these
+matrices)."""
 import os
 import shutil
 import subprocess
@@ -25,4 +29,4 @@ def test_host_layout_builder_invariants(tmp_path):
     subprocess.run([cxx, "-std=c++17", "-O2", "-pthread", "-I", os.path.join(ROOT, "pdos_gb300", "csrc"),
                     os.path.join(ROOT, "tests", "batch_layout_check.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
-    assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout[-3000:]
+    assert r.returncode == 0 and r.stdout.strip().splitlines()[-1].startswith("OK"), r.stdout[-3000:]
