@@ -5,6 +5,7 @@
 // solver does, and checks every structural promise the kernels rely on,
 // including the lane-to-row map of instances that sort their rows.
 // Prints "OK" and exits 0, or prints the first failures and exits 1.
+#include <cmath>
 #include <cstdio>
 #include <random>
 #include <vector>
@@ -144,6 +145,64 @@ int main() {
     for (int64_t r = 0; r < m; ++r) CHECK(seen[r] == 1, "instance %d row %lld covered %d times", i, (long long)r, seen[r]);
   }
   CHECK(nsplit_total > 0, "no split rows were exercised");
+  // run the layout as the kernels do -- slices (lane -> row, natural or
+  // through slice_row), pieces (a warp's sum, whole rows to the epilogue,
+  // split rows' partials summed in order) -- and compare with a direct CSR
+  // product
+  {
+    std::vector<double> val(col.size()), x(c0.back());
+    std::mt19937 gv(3);
+    std::uniform_real_distribution<double> u(-1.0, 1.0);
+    for (auto &v : val) v = u(gv);
+    for (auto &v : x) v = u(gv);
+    for (int i = 0; i < count; ++i) {
+      const Side &sd = sides[i];
+      const int64_t m = r0[i + 1] - r0[i];
+      std::vector<double> y(m, std::nan("")), part(sd.npieces, 0.0);
+      for (int s = 0; s < sd.nslices; ++s) {
+        const int64_t k = sd.slice0 + s;
+        const int w = hb.slice_w[k], width = w < 0 ? -w : w;
+        for (int lane = 0; lane < 32; ++lane) {
+          if ((hb.slice_skip[k] >> lane) & 1u) continue;
+          double acc = 0.0;
+          for (int c = 0; c < width; ++c) {
+            const int64_t e = w < 0 ? hb.slice_beg[k] + 128LL * (c / 4) + 4 * lane + c % 4
+                                    : hb.slice_beg[k] + 32LL * c + lane;
+            if (hb.src[e] >= 0) acc = std::fma(val[hb.src[e]], x[c0[i] + hb.idx[e]], acc);
+          }
+          const int64_t r = sd.sorted ? (int64_t)hb.slice_row[(size_t)k * 32 + lane] : 32LL * s + lane;
+          y[r] = acc;
+        }
+      }
+      for (int q = 0; q < sd.npieces; ++q) {
+        const int64_t pk = sd.piece0 + q;
+        double acc = 0.0;
+        for (int e = 0; e < hb.piece_len[pk]; ++e) {
+          const int64_t at = hb.piece_beg[pk] + e;
+          if (hb.src[at] >= 0) acc += val[hb.src[at]] * x[c0[i] + hb.idx[at]];
+        }
+        if (hb.piece_row[pk] >= 0)
+          y[hb.piece_row[pk]] = acc;
+        else
+          part[q] = acc;
+      }
+      for (int q = 0; q < sd.nsplit; ++q) {
+        const int64_t sk = sd.split0 + q;
+        double acc = 0.0;
+        for (int t = 0; t < hb.split_np[sk]; ++t) acc += part[hb.split_p0[sk] + t];
+        y[hb.split_row[sk]] = acc;
+      }
+      for (int64_t r = 0; r < m; ++r) {
+        double d = 0.0, mag = 0.0;
+        for (int64_t e = ptr[r0[i] + r]; e < ptr[r0[i] + r + 1]; ++e) {
+          d += val[e] * x[col[e]];
+          mag += std::fabs(val[e] * x[col[e]]);
+        }
+        CHECK(std::fabs(y[r] - d) <= 1e-12 * (1.0 + mag), "instance %d row %lld: layout product %.17g, direct %.17g",
+              i, (long long)r, y[r], d);
+      }
+    }
+  }
   // sorted instances: inside each window of rows, slice lanes hold rows in
   // order of decreasing length
   int nsorted = 0;
