@@ -32,9 +32,13 @@ struct Side {
 };
 
 // Rows sorted by length inside windows of this many rows when an
-// instance's slices would otherwise pay more than kSortPadding of padding.
+// instance's slices would otherwise pay more than kSortPadding of padding
+// and the side holds at least kSortMinNnz nonzeros: a smaller instance is
+// bound by latency, not by the bytes padding adds, and its epilogue would
+// reach its rows out of order.
 constexpr int kSortWindow = 1024;
 constexpr double kSortPadding = 0.15;
+constexpr int64_t kSortMinNnz = 32768;
 
 // Work over instances on the host's cores (atomic counter, no exceptions).
 template <class F>
@@ -82,8 +86,9 @@ struct Cursor {
 // Slices hold an instance's short rows (at most long_row nonzeros) 32 at a
 // time, lane = row, padded to the slice's longest row.  In natural order a
 // slice also keeps a lane for each long row and each row past the end
-// (skipped).  When that order pays more than kSortPadding of padding and
-// sorting saves a tenth of the elements, the short rows are instead sorted
+// (skipped).  When that order pays more than kSortPadding of padding, the
+// instance is large enough (kSortMinNnz) and sorting saves a tenth of the
+// elements, the short rows are instead sorted
 // by length (longest first, stable) inside windows of kSortWindow rows and
 // packed densely; slice_row then gives each lane's row.  Each row keeps its
 // own entries in its own lane in their order, so its sum is the same chain
@@ -158,7 +163,7 @@ struct HybBuild {
         lanes[r] = (int32_t)r;
         useful += len_of(r);
       }
-    if (sort_rows && R > 32) {
+    if (sort_rows && R > 32 && ptr[r1] - ptr[r0] >= kSortMinNnz) {
       const int64_t natural = slice_elems(lanes);
       if (natural - useful > kSortPadding * natural) {
         std::vector<int32_t> sorted;

@@ -7,11 +7,10 @@ does, and checks what the batch kernel relies on.  Every nonzero is placed
 exactly once, with its instance-local index.  Every row is covered exactly
 once: by a slice lane, by one piece, or by the pieces of a split record.
 Slices and pieces are 4-aligned and within their width and length limits,
-and padding is marked.  Instances whose natural row order pays much padding
-sort their short rows by length inside windows: their lanes map to rows
-through slice_row, only their last slice skips lanes, and their layouts are
-smaller than the natural-order ones (57 % padding down to about 6 % on these
-matrices).  Finally the layout is run on the CPU as the kernels run it
+and padding is marked.  Large instances whose natural row order pays much
+padding sort their short rows by length inside windows: their lanes map to
+rows through slice_row, only their last slice skips lanes, and the layouts
+are smaller than the natural-order ones.  Finally the layout is run on the CPU as the kernels run it
 (slice lanes through their row map, pieces, split rows summed in order) and
 its product compared with a direct CSR product."""
 import os
